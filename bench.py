@@ -1,0 +1,357 @@
+"""Throughput of the QMIV metric path on one GB300 (or N, one process per GPU).
+
+Workload (one "step"): the multi-view set of 12 views x 8 frames of 10-bit 4:2:0 picture
+pairs — 3 equirectangular views 4096x2048 (WS-PSNR rows weighted, IV-PSNR weighted), 6
+perspective views 1920x1080, 3 at 2048x1088 — each pair getting GCD, PSNR, WS-PSNR and
+IV-PSNR (search range 2) in one batched launch sequence. Inputs are seeded synthetic
+pictures (ivpsnr_gb300.synth) with block shifts, offsets, noise and elliptical holes.
+
+value: Gpixel/s (luma pixels of all pairs / device time), inputs resident in HBM; the
+inputs (2.1 GB) exceed the 129 MB L2, so no flush is needed between steps.
+e2e: the same metric with the inputs copied from pinned host memory every step and the
+per-frame results read back, through the C ABI.
+--impl reference: the CPU restatement of the reference path (oracle/) on all host cores,
+one picture pair of the workload per step.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "IV-PSNR & IV-SSIM Gpixel/s on 1 GB300: batched vs plain at exact match; bwd ms"
+VIEWS = [(4096, 2048, True)] * 3 + [(1920, 1080, False)] * 6 + [(2048, 1088, False)] * 3
+FRAMES = 8
+BD = 10
+WORKLOAD = "multiview-ivpsnr-wspsnr-10bit-420: 3x4096x2048 ERP + 6x1920x1080 + 3x2048x1088, 8 frames, SR 2"
+
+
+def jobs_list():
+    out = []
+    for v, (w, h, erp) in enumerate(VIEWS):
+        for f in range(FRAMES):
+            out.append((v, f, w, h, erp))
+    return out
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region."""
+    FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def make_inputs(jobs, pinned=True):
+    import torch
+    from ivpsnr_gb300 import synth
+    host = []
+    for (v, f, w, h, erp) in jobs:
+        n = w * h + 2 * (w // 2) * (h // 2)
+        ref = torch.empty(n, dtype=torch.int16, pin_memory=pinned).numpy().view(np.uint16)
+        tst = torch.empty(n, dtype=torch.int16, pin_memory=pinned).numpy().view(np.uint16)
+        synth.pair420(w, h, BD, seed=synth.seed_for(1, v, f), noise_sigma=2.0, offset=(3.0, -2.0, 1.0),
+                      holes=True, out=(ref, tst))
+        host.append((ref, tst))
+    return host
+
+
+def run_reference(args):
+    """CPU restatement of the reference path on all host cores (the oracle port)."""
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from ivpsnr_gb300 import synth
+    from oracle import oracle as oq
+    nth = os.cpu_count() or 1
+    jobs = jobs_list()
+
+    def step(i):
+        v, f, w, h, erp = jobs[(i * FRAMES) % len(jobs)]
+        ref, tst = synth.pair420(w, h, BD, seed=synth.seed_for(1, v, f), holes=True)
+        p0 = oq.upsample420(synth.split420(ref, w, h), w, h)
+        p1 = oq.upsample420(synth.split420(tst, w, h), w, h)
+        t = time.perf_counter()
+        oq.frame(p0, p1, BD, False, use_ws=erp, nthreads=nth)
+        return w * h, time.perf_counter() - t
+
+    for i in range(args.warmup):
+        step(i)
+    px, secs = 0, 0.0
+    for i in range(args.steps):
+        a, b = step(args.warmup + i)
+        px += a
+        secs += b
+    val = px / secs / 1e9
+    sample = "one picture pair per step (views cycled), GCD+PSNR+WS-PSNR+IV-PSNR, %d host threads" % nth
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "Gpixel/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+        "config": {"workload": WORKLOAD},
+        "cpu_baseline": {"value": val, "unit": "Gpixel/s", "cores": nth, "kind": "port", "sample": sample},
+        "e2e": {"value": val, "unit": "Gpixel/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def cpu_baseline_sample():
+    """Bounded CPU sample for the GPU line: two pairs (one ERP, one 1080p) on all host cores."""
+    from ivpsnr_gb300 import synth
+    from oracle import oracle as oq
+    nth = os.cpu_count() or 1
+    px, secs = 0, 0.0
+    for (v, w, h, erp) in [(0, 4096, 2048, True), (3, 1920, 1080, False)]:
+        ref, tst = synth.pair420(w, h, BD, seed=synth.seed_for(1, v, 0), holes=True)
+        p0 = oq.upsample420(synth.split420(ref, w, h), w, h)
+        p1 = oq.upsample420(synth.split420(tst, w, h), w, h)
+        t = time.perf_counter()
+        oq.frame(p0, p1, BD, False, use_ws=erp, nthreads=nth)
+        secs += time.perf_counter() - t
+        px += w * h
+    return {"value": px / secs / 1e9, "unit": "Gpixel/s", "cores": nth, "kind": "port",
+            "sample": "2 of 96 picture pairs (4096x2048 ERP + 1920x1080), GCD+PSNR+WS-PSNR+IV-PSNR, oracle/ C port"}
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import ivpsnr_gb300 as q
+    from ivpsnr_gb300 import _abi, synth
+
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    jobs = jobs_list()
+    host = make_inputs(jobs)
+    devbufs = []
+    for (ref, tst) in host:
+        devbufs.append((torch.from_numpy(ref.view(np.int16)).to(dev), torch.from_numpy(tst.view(np.int16)).to(dev)))
+    torch.cuda.synchronize()
+
+    def planes(t, w, h):
+        a = w * h
+        ca = (w // 2) * (h // 2)
+        return [t[:a].view(h, w), t[a:a + ca].view(h // 2, w // 2), t[a + ca:].view(h // 2, w // 2)]
+
+    qjobs = []
+    for (v, f, w, h, erp), (d0, d1) in zip(jobs, devbufs):
+        j = _abi.Job()
+        j.pic0 = q.make_pic(planes(d0, w, h), BD)
+        j.pic1 = q.make_pic(planes(d1, w, h), BD)
+        j.pic0.sample_bytes = 2
+        j.pic1.sample_bytes = 2
+        j.metrics = q.M_PSNR | q.M_WSPSNR | q.M_IVPSNR
+        j.use_ws = int(erp)
+        qjobs.append(j)
+    nres = len(qjobs)
+    rsz = ctypes.sizeof(_abi.FrameResult)
+    res_dev = torch.zeros(nres * rsz, dtype=torch.uint8, device=dev)
+    res_host = torch.zeros(nres * rsz, dtype=torch.uint8, pin_memory=True)
+    P = q.Processor(4096, 2048, max_jobs=nres)
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    # ---- device-resident batched throughput ----
+    for _ in range(args.warmup):
+        P.calc_batch(qjobs, res_dev.data_ptr(), sptr)
+    torch.cuda.synchronize()
+    launches0 = P.kernel_launches()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        P.calc_batch(qjobs, res_dev.data_ptr(), sptr)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    clk = clocks.stop()
+    gpu_launches = P.kernel_launches() - launches0
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    px_per_step = sum(w * h for (_, _, w, h, _) in jobs)
+    value = px_per_step * world / (ms * 1e-3) / 1e9
+
+    # correctness spot check of the timed results against the oracle on one small view
+    res_host.copy_(res_dev)
+    r0 = _abi.FrameResult.from_buffer_copy(bytes(res_host[:rsz].numpy()))
+
+    # ---- per-kernel device time (CUDA events on the launching stream) ----
+    P.set_profiling(True)
+    ktimes = {}
+    for _ in range(3):
+        P.calc_batch(qjobs, res_dev.data_ptr(), sptr)
+        for name, t in P.kernel_times():
+            ktimes.setdefault(name, []).append(t)
+    P.set_profiling(False)
+    kavg = {k: float(np.mean(v)) for k, v in ktimes.items()}
+    cps_name = max(kavg, key=kavg.get)
+    cps_ms = kavg[cps_name]
+    in_bytes = sum(2 * (w * h + 2 * (w // 2) * (h // 2)) * 2 for (_, _, w, h, _) in jobs)
+    hbm_peak, peak_kind = peaks()
+    achieved = in_bytes / (cps_ms * 1e-3) / 1e9
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "cps_traffic.json")
+    if os.path.exists(tf):
+        try:
+            d = json.load(open(tf))
+            traffic = d["dram_bytes_per_pixel"] * px_per_step
+        except Exception:
+            traffic = None
+    # integer-pipe view: algorithmic ops per candidate (3 sub, 3 mul, 2 add/mad, 1 compare-select)
+    # plus ~10 per pixel for the argmin re-diff and accumulate, both directions
+    alg_ops = px_per_step * 2 * (25 * 9 + 10)
+    sm_mhz = clk.get("sm_mhz") or 1900.0
+    int_peak = 152 * 128 * sm_mhz * 1e6  # INT32 lanes x clock (derived from the sampled clock)
+
+    # ---- plain per-frame form: one qmiv_calc_frame per pair (device inputs) ----
+    Pp = q.Processor(4096, 2048, max_jobs=1)
+    plain_pics = [(j.pic0, j.pic1, erp) for j, (_, _, _, _, erp) in zip(qjobs, jobs)]
+    Pws = q.Processor(4096, 2048, max_jobs=1, use_ws=True)
+    def plain_pass():
+        for p0, p1, erp in plain_pics:
+            (Pws if erp else Pp).calc_frame(p0, p1, q.M_PSNR | q.M_WSPSNR | q.M_IVPSNR, sptr)
+    plain_pass()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    plain_pass()
+    torch.cuda.synchronize()
+    plain_ms = (time.perf_counter() - t) * 1e3
+    plain_value = px_per_step / (plain_ms * 1e-3) / 1e9
+
+    # ---- end to end: pinned host inputs copied every step, results read back ----
+    h2d = sum(r.nbytes + t_.nbytes for (r, t_) in host)
+    def e2e_step():
+        for (ref, tst), (d0, d1) in zip(host, devbufs):
+            d0.copy_(torch.from_numpy(ref.view(np.int16)), non_blocking=True)
+            d1.copy_(torch.from_numpy(tst.view(np.int16)), non_blocking=True)
+        P.calc_batch(qjobs, res_dev.data_ptr(), sptr)
+        res_host.copy_(res_dev, non_blocking=True)
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    e2e_value = px_per_step * world / (e2e_ms * 1e-3) / 1e9
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "Gpixel/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "pairs": len(jobs), "luma_pixels_per_step": px_per_step,
+                       "bitdepth": BD, "chroma": "4:2:0", "search_range": 2,
+                       "l2": "inputs %.2f GB per step > 129 MB L2; no flush" % (in_bytes / 1e9)},
+            "clocks": clk,
+            "e2e": {"value": e2e_value, "unit": "Gpixel/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": nres * rsz},
+            "gpu_launches": gpu_launches,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "traffic": traffic, "kernel": cps_name,
+                         "kernel_ms": cps_ms, "peak_kind": peak_kind},
+            "roofline_int": {"bound": "int32 issue", "achieved_tops": alg_ops / (cps_ms * 1e-3) / 1e12,
+                             "peak_tops": int_peak / 1e12, "frac": alg_ops / (cps_ms * 1e-3) / int_peak,
+                             "peak_kind": "152 SMs x 128 INT32 lanes x sampled SM clock"},
+            "kernel_ms": kavg,
+            "plain": {"value": plain_value, "unit": "Gpixel/s", "batched_over_plain": value / world / plain_value},
+            "check": {"ivpsnr_pair0": r0.ivpsnr, "gcd_pair0": list(r0.gcd_r2t)[:3]},
+        }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline_sample()
+        print(json.dumps(line))
+    P.close()
+    Pp.close()
+    Pws.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,203 @@
+/*
+ * qmiv_gb300 — C ABI of the GB300 implementation of the QMIV metric path
+ * (IV-PSNR, PSNR, WS-PSNR, SSIM, MS-SSIM, IV-SSIM; reference: jstankowski/ivpsnr,
+ * libs/pmbb-ivqm).
+ *
+ * Plain pointers and sizes only. Every call returns a qmiv_status; nothing throws.
+ * A handle is not thread-safe; several handles (one per host thread or stream) may be
+ * used at once. The handle owns all device scratch, sized at qmiv_create for the
+ * largest picture and batch it will see; the calc calls allocate nothing.
+ *
+ * Each entry point names the reference interface it replaces (file:line within the
+ * reference project). Picture 0 / picture 1 are the application's two inputs
+ * (-i0 / -i1 of apps/QMIV, read into m_PicInP[0] / m_PicInP[1]); every metric is
+ * computed with the argument order the application uses (apps/QMIV/src/xAppQMIV.cpp:693-935).
+ */
+#ifndef QMIV_GB300_H
+#define QMIV_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QMIV_ABI_VERSION 1
+
+typedef enum qmiv_status {
+  QMIV_OK             = 0,
+  QMIV_BAD_ARG        = 1, /* null pointer, size out of range, stride < width, ... */
+  QMIV_UNSUPPORTED    = 2, /* valid request this build does not implement (e.g. odd 4:2:0 sizes) */
+  QMIV_CUDA_ERROR     = 3, /* a CUDA runtime call failed; qmiv_last_error() has the text */
+  QMIV_DEVICE_TIMEOUT = 4, /* a bounded device-side wait gave up */
+  QMIV_OUT_OF_MEMORY  = 5,
+  QMIV_TOO_LARGE      = 6  /* picture or batch larger than the handle was created for */
+} qmiv_status;
+
+/* Metric selection bits (apps/QMIV/src/xAppQMIV.h:140-153, eMetric) */
+enum {
+  QMIV_M_PSNR   = 1u << 0,
+  QMIV_M_WSPSNR = 1u << 1,
+  QMIV_M_IVPSNR = 1u << 2,
+  QMIV_M_SSIM   = 1u << 3,
+  QMIV_M_MSSSIM = 1u << 4,
+  QMIV_M_IVSSIM = 1u << 5,
+  QMIV_M_ALL    = 0x3Fu
+};
+
+enum { QMIV_CF420 = 420, QMIV_CF444 = 444 };
+enum { QMIV_SSIM_REF10 = 0 /* the reference's truncated 10x10 window */, QMIV_SSIM_GAUSS11 = 1 /* full 11x11 */ };
+
+/* One picture: three planes of 8-bit or 16-bit samples (little endian), host or device.
+ * For 4:2:0 the chroma planes are (width/2) x (height/2) and are upsampled by
+ * nearest neighbour on the fly, as xSeq::xUnpackFrame does (libs/pmbb-core/src/xSeq.cpp:179-213).
+ * For 4:4:4 the planes may be the reference's xPicP planes (xPic.h:18): pass the origin
+ * pointers and the stride; the margin is not read (window reads clamp to the picture,
+ * which equals the reference's edge-replicated margin). */
+typedef struct qmiv_pic {
+  const void* plane[3];    /* Y, Cb, Cr */
+  int32_t     stride[3];   /* in samples */
+  int32_t     width, height;
+  int32_t     bitdepth;    /* 8..14; the sample type is set by sample_bytes */
+  int32_t     sample_bytes;/* 1 (uint8) or 2 (uint16) */
+  int32_t     chroma_format; /* QMIV_CF420 or QMIV_CF444 */
+  int32_t     is_device;   /* 1: device pointers; 0: host pointers (copied by the call) */
+} qmiv_pic;
+
+/* Processor parameters (xCorrespPixelShift.h:28-45, xGlobClrDiff.h:17-25,
+ * xWeightedSpherically.h:21, xPSNR.h:31, xWSPSNR.h:28). */
+typedef struct qmiv_options {
+  int32_t search_range;    /* default 2 */
+  int32_t cmp_w_search[4]; /* default 4,1,1,0 */
+  int32_t cmp_w_avg[4];    /* default 4,1,1,0 */
+  float   unnoticeable[4]; /* default 0.01,0.01,0.01,0 */
+  int32_t use_ws;          /* equirectangular weighting of the PSNR family (initWS) */
+  int32_t lon_deg, lat_deg;/* default 360, 180 */
+  int32_t fake_exact;      /* 1 (default): exact components report PSNR(SSD=1) as the application does */
+  int32_t legacy_ws8;      /* setLegacyWS8bit (off by default, never set by the application) */
+  int32_t ssim_window;     /* QMIV_SSIM_REF10 (default) or QMIV_SSIM_GAUSS11 */
+} qmiv_options;
+
+/* Per-frame results. Per-component arrays hold Y, Cb, Cr (index 3 unused, 0). The *_pic
+ * values are the application's 4:1:1 weighted per-picture values (xAppQMIV.h:245-251). */
+typedef struct qmiv_frame_result {
+  uint32_t metrics;        /* QMIV_M_* bits computed */
+  int32_t  status;         /* device-side status of this frame (qmiv_status) */
+  int32_t  gcd_r2t[4];     /* global colour difference, xGlobClrDiffProc::CalcGlobalColorDiff(P0,P1) */
+  int32_t  exact[4];       /* component identical in both pictures */
+  double   psnr[4], psnr_pic;
+  double   wspsnr[4], wspsnr_pic;
+  double   ivpsnr, ivpsnr_r2t, ivpsnr_t2r;
+  uint64_t sse_r2t[4], sse_t2r[4]; /* exact CPS squared-error sums per component */
+  double   ssim[4], ssim_pic;
+  double   msssim[4], msssim_pic;
+  double   ivssim, ivssim_r2t, ivssim_t2r;
+} qmiv_frame_result;
+
+/* Per-sequence averages (xMetricStat::calcAvgMetric, xAppQMIV.h:256-260). */
+typedef struct qmiv_seq_result {
+  int32_t  num_frames;
+  uint32_t metrics;
+  double   psnr[4], psnr_pic, wspsnr[4], wspsnr_pic, ivpsnr;
+  double   ssim[4], ssim_pic, msssim[4], msssim_pic, ivssim;
+} qmiv_seq_result;
+
+/* One job of a batch: a picture pair plus the metrics to compute on it. Pictures of a
+ * batch may differ in size, bit depth and chroma format; use_ws selects ERP weighting
+ * per job (lat_deg from the options). Device pointers only. */
+typedef struct qmiv_job {
+  qmiv_pic pic0, pic1;
+  uint32_t metrics;
+  int32_t  use_ws;
+  /* optional device outputs of the shift-compensated pictures (4:4:4 uint16, stride in
+   * samples; null to skip): scp0 is built from picture 0, scp1 from picture 1 */
+  uint16_t* scp0[3];
+  uint16_t* scp1[3];
+  int32_t   scp_stride;
+} qmiv_job;
+
+typedef struct qmiv_handle qmiv_handle;
+typedef struct CUstream_st* qmiv_stream; /* a cudaStream_t; 0 = legacy default stream */
+
+/* --- version / errors ------------------------------------------------------------- */
+int32_t     qmiv_abi_version(void);
+const char* qmiv_status_str(qmiv_status s);
+const char* qmiv_last_error(void); /* thread-local text of the last failure */
+
+/* --- processors: create/destroy ------------------------------------------------------
+ * Replaces the processor set-up of apps/QMIV/src/xAppQMIV.cpp:593-650 (xIVPSNR / xSSIM /
+ * xIVSSIM ::create, setSearchRange, setCmpWeights*, setUnntcbCoef, initWS, initRowBuffers,
+ * initThreadPool). max_jobs bounds qmiv_calc_batch. */
+void        qmiv_default_options(qmiv_options* opt);
+qmiv_status qmiv_create(qmiv_handle** out, const qmiv_options* opt, int32_t max_width, int32_t max_height,
+                        int32_t max_jobs);
+qmiv_status qmiv_destroy(qmiv_handle* h);
+qmiv_status qmiv_set_options(qmiv_handle* h, const qmiv_options* opt);
+
+/* --- per frame -----------------------------------------------------------------------
+ * All metrics of one picture pair in one call: replaces the per-frame body of
+ * xAppQMIV::processAllFrames (xAppQMIV.cpp:661-751): GCD (:693-697), SCP (:703), and
+ * calcFrame____PSNR / __WSPSNR / __IVPSNR / ____SSIM / __MSSSIM / __IVSSIM (:831-935).
+ * Enqueued on `stream`; returns once the results are in *out (synchronous, like the
+ * reference's calcPic* calls). The frame is also added to the sequence statistics. */
+qmiv_status qmiv_calc_frame(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, uint32_t metrics,
+                            qmiv_frame_result* out, qmiv_stream stream);
+
+/* Batched form: n jobs of mixed sizes in one launch sequence on `stream`, asynchronous.
+ * results (n entries) must be device memory or host memory the device can write
+ * (cudaHostAlloc'd); they are valid after the stream synchronises. Frames are not added
+ * to the sequence statistics. */
+qmiv_status qmiv_calc_batch(qmiv_handle* h, const qmiv_job* jobs, int32_t n, qmiv_frame_result* results,
+                            qmiv_stream stream);
+
+/* --- fine-grained calls (each synchronous; for the C++ processor shim) --------------- */
+/* xGlobClrDiffProc::CalcGlobalColorDiff(P0, P1) (xGlobClrDiff.h:41 -> xGlobClrDiff.cpp:15) */
+qmiv_status qmiv_gcd(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, int32_t gcd_r2t[4],
+                     qmiv_stream stream);
+/* xPSNR::calcPicPSNR (xPSNR.cpp:17) and xWSPSNR::calcPicWSPSNR (xWSPSNR.cpp:17) */
+qmiv_status qmiv_psnr(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, double psnr[4],
+                      double wspsnr[4], qmiv_stream stream);
+/* xIVPSNR::calcPicIVPSNR(Tst=P0, Ref=P1, GCD) (xIVPSNR.cpp:32-56); gcd_r2t may be null (computed) */
+qmiv_status qmiv_ivpsnr(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, const int32_t* gcd_r2t,
+                        double* ivpsnr, double* r2t, double* t2r, qmiv_stream stream);
+/* xShftCompPic::GenShftCompPics(&SCP1, &SCP0, &P1, &P0, GCD) (xShftCompPic.cpp:12-20); outputs are
+ * host or device 4:4:4 uint16 planes per scp_is_device */
+qmiv_status qmiv_scp(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, const int32_t* gcd_r2t,
+                     uint16_t* scp0[3], uint16_t* scp1[3], int32_t scp_stride, int32_t scp_is_device,
+                     qmiv_stream stream);
+/* xSSIM::calcPicSSIM(Tst, Ref, CalcL) (xSSIM.cpp:54) on any two pictures (e.g. P0 and SCP1) */
+qmiv_status qmiv_ssim(qmiv_handle* h, const qmiv_pic* tst, const qmiv_pic* ref, int32_t calc_l, double ssim[4],
+                      qmiv_stream stream);
+/* xSSIM::calcPicMSSSIM (xSSIM.cpp:67-87) */
+qmiv_status qmiv_msssim(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, double msssim[4],
+                        qmiv_stream stream);
+/* xIVSSIM::calcPicIVSSIM(P0, P1, SCP0, SCP1) (xSSIM.cpp:192-210), building the SCPs itself */
+qmiv_status qmiv_ivssim(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, const int32_t* gcd_r2t,
+                        double* ivssim, double* r2t, double* t2r, qmiv_stream stream);
+
+/* --- per sequence ----------------------------------------------------------------------
+ * xMetricStat::calcAvgMetric (xAppQMIV.h:256-260): compensated mean over the frames passed
+ * to qmiv_calc_frame since create or the last reset. */
+qmiv_status qmiv_finish_sequence(qmiv_handle* h, qmiv_seq_result* out);
+qmiv_status qmiv_reset_sequence(qmiv_handle* h);
+
+/* --- introspection (tests, profiling) -------------------------------------------------- */
+/* Number of kernels this handle has launched since creation. */
+int64_t     qmiv_kernel_launches(const qmiv_handle* h);
+/* CPS kernel variants (tile shape, search-window unrolling, key width): count, name, and
+ * a per-handle override used by the autotuner and the tests (-1 restores the default
+ * choice; a variant that does not fit a job falls back to the default for that job). */
+int32_t     qmiv_cps_variant_count(void);
+const char* qmiv_cps_variant_name(int32_t v);
+qmiv_status qmiv_set_cps_variant(qmiv_handle* h, int32_t v);
+/* Per-kernel timing of the most recent calc call (CUDA events recorded on the call's
+ * stream around each launch, when enabled). qmiv_kernel_times synchronises with those
+ * events and returns up to max launches: names[i] (static strings) and ms[i]. */
+qmiv_status qmiv_set_profiling(qmiv_handle* h, int32_t enable);
+int32_t     qmiv_kernel_times(qmiv_handle* h, const char** names, double* ms, int32_t max);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,235 @@
+// Picture statistics kernel: per-row sums of differences and squared differences of the
+// two input pictures, read once from their native layout (8/16-bit, 4:2:0 or 4:4:4).
+// Its last block per job turns the rows into
+//   * the global colour difference GCD_R2T (libs/pmbb-ivqm/src/xGlobClrDiff.cpp:15-48 with
+//     the application's argument order, xGlobClrDiff.h:41),
+//   * PSNR (xPSNR.cpp:17-36,93-111,139-146) with the application's exact-component
+//     replacement (apps/QMIV/src/xAppQMIV.cpp:837-844),
+//   * WS-PSNR (xWSPSNR.cpp:17-48,101-125).
+// HBM-bound: each sample of both pictures is read once (1.5 samples per luma pixel for
+// 4:2:0). For 4:2:0 the chroma sums of the 4:4:4 picture the reference works on are exact
+// multiples of the native chroma sums (each chroma sample is replicated 2x2,
+// xPixelOpsSTD.cpp:30-49), so the upsampled planes are never formed.
+#include "qmiv_device.cuh"
+
+namespace qmiv {
+
+namespace {
+
+constexpr int kStatsThreads = 256;
+
+// sum(a-b) and sum((a-b)^2) over n samples of two rows
+template <typename T>
+__device__ __forceinline__ void row_stats(const T* __restrict__ a, const T* __restrict__ b, int n, bool vec,
+                                          int& sd, unsigned long long& ssd)
+{
+  int i0 = 0;
+  if(vec)
+  { // 16-byte loads: 8 uint16 or 16 uint8 samples per load
+    constexpr int V = 16 / sizeof(T);
+    const int nv = n / V;
+    const uint4* av = reinterpret_cast<const uint4*>(a);
+    const uint4* bv = reinterpret_cast<const uint4*>(b);
+    for(int i = threadIdx.x; i < nv; i += blockDim.x)
+    {
+      const uint4 x = __ldg(av + i), y = __ldg(bv + i);
+      const T* xs = reinterpret_cast<const T*>(&x);
+      const T* ys = reinterpret_cast<const T*>(&y);
+      unsigned int q = 0;
+      #pragma unroll
+      for(int k = 0; k < V; k++) { const int d = (int)xs[k] - (int)ys[k]; sd += d; q += (unsigned int)(d * d); }
+      ssd += q;
+    }
+    i0 = nv * V;
+  }
+  for(int i = i0 + threadIdx.x; i < n; i += blockDim.x)
+  {
+    const int d = (int)a[i] - (int)b[i];
+    sd += d; ssd += (unsigned long long)(d * d);
+  }
+}
+
+template <typename T>
+__device__ void stats_rowpair(const DevJob& J, int y, bool vec, int sd[2][3], unsigned long long ssd[2][3])
+{
+  const T* p0[3]; const T* p1[3];
+  for(int c = 0; c < 3; c++) { p0[c] = (const T*)J.p0[c]; p1[c] = (const T*)J.p1[c]; }
+  for(int r = 0; r < 2; r++)
+  {
+    if(y + r >= J.H) break;
+    row_stats<T>(p1[0] + (int64_t)(y + r) * J.stride1[0], p0[0] + (int64_t)(y + r) * J.stride0[0], J.W, vec, sd[r][0], ssd[r][0]);
+  }
+  if(J.cshift)
+  { // one chroma row serves luma rows y and y+1
+    const int cy = y >> 1, cw = J.W >> 1;
+    for(int c = 1; c < 3; c++)
+      row_stats<T>(p1[c] + (int64_t)cy * J.stride1[c], p0[c] + (int64_t)cy * J.stride0[c], cw, vec, sd[0][c], ssd[0][c]);
+  }
+  else
+  {
+    for(int r = 0; r < 2; r++)
+    {
+      if(y + r >= J.H) break;
+      for(int c = 1; c < 3; c++)
+        row_stats<T>(p1[c] + (int64_t)(y + r) * J.stride1[c], p0[c] + (int64_t)(y + r) * J.stride0[c], J.W, vec, sd[r][c], ssd[r][c]);
+    }
+  }
+}
+
+__device__ bool vec_ok(const DevJob& J)
+{
+  const int sb = J.sbytes;
+  for(int c = 0; c < 3; c++)
+  {
+    if((((uintptr_t)J.p0[c]) | ((uintptr_t)J.p1[c])) & 15) return false;
+    if(((J.stride0[c] * sb) | (J.stride1[c] * sb)) & 15) return false;
+  }
+  return true;
+}
+
+// Last block of a job: GCD, exact flags, PSNR, WS-PSNR.
+__device__ void finalize_stats(const DevJob& J, const Params& p, double* scratch)
+{
+  __shared__ long long s_sd[3];
+  __shared__ unsigned long long s_ssd[3];
+  const int64_t area = (int64_t)J.W * J.H;
+  for(int c = 0; c < 3; c++)
+  {
+    long long sd = 0; unsigned long long ssd = 0;
+    for(int y = threadIdx.x; y < J.H; y += blockDim.x)
+    {
+      sd  += __ldcg(J.stat_rows + (int64_t)y * 6 + c);
+      ssd += (unsigned long long)__ldcg(J.stat_rows + (int64_t)y * 6 + 3 + c);
+    }
+    sd = warp_sum(sd); ssd = warp_sum(ssd);
+    __syncthreads();
+    if((threadIdx.x & 31) == 0) { scratch[2 * (threadIdx.x >> 5)] = __longlong_as_double(sd); scratch[2 * (threadIdx.x >> 5) + 1] = __longlong_as_double((long long)ssd); }
+    __syncthreads();
+    if(threadIdx.x == 0)
+    {
+      long long a = 0; unsigned long long b = 0;
+      for(int w = 0; w < (int)(blockDim.x >> 5); w++) { a += __double_as_longlong(scratch[2 * w]); b += (unsigned long long)__double_as_longlong(scratch[2 * w + 1]); }
+      s_sd[c] = a; s_ssd[c] = b;
+    }
+    __syncthreads();
+  }
+
+  double ws[3] = { 0, 0, 0 };
+  if(J.use_ws && (J.metrics & QMIV_M_WSPSNR))
+  {
+    for(int c = 0; c < 3; c++)
+    {
+      Kbns k = { 0.0, 0.0 };
+      for(int y = threadIdx.x; y < J.H; y += blockDim.x)
+        k = kbns_add(k, __dmul_rn((double)(unsigned long long)__ldcg(J.stat_rows + (int64_t)y * 6 + 3 + c), J.ws[y]));
+      ws[c] = block_kbns(k, scratch);
+    }
+  }
+
+  if(threadIdx.x == 0)
+  {
+    qmiv_frame_result* R = J.result;
+    const int mx = (1 << J.bd) - 1;
+    int32_t g[4] = { 0, 0, 0, 0 };
+    for(int c = 0; c < 3; c++)
+    { // rne(sum / area) clipped to +-rne_f32(unc*Max) (xGlobClrDiff.cpp:21,43-45)
+      const int md = p.maxdiff_for_bd[J.bd][c];
+      int v = __double2int_rn(__ddiv_rn((double)s_sd[c], (double)area));
+      g[c] = v < -md ? -md : (v > md ? md : v);
+    }
+    if(!J.gcd_given) { for(int c = 0; c < 4; c++) J.sc->gcd[c] = g[c]; }
+    double ps[3], wp[3];
+    const double fake = psnr_from_ssd(1.0, area, J.bd);
+    for(int c = 0; c < 3; c++)
+    {
+      const bool exact = s_ssd[c] == 0;
+      R->exact[c] = exact;
+      ps[c] = psnr_from_ssd((double)s_ssd[c], area, J.bd);
+      if(J.use_ws) { const double e = __dmul_rn(ws[c], J.ws_corr); wp[c] = psnr_from_ssd(e, area, J.bd); }
+      else wp[c] = ps[c];
+      if(exact && p.fake_exact) { ps[c] = fake; wp[c] = fake; }
+    }
+    if(J.use_ws && p.legacy_ws8 && J.bd == 10)
+    { // xWSPSNR.cpp:34-46
+      const double real = (double)mx, fk = (double)(255 << 2);
+      const double mod = __dmul_rn(10.0, __dsub_rn(log10(__dmul_rn(real, real)), log10(__dmul_rn(fk, fk))));
+      for(int c = 0; c < 3; c++) wp[c] = __dsub_rn(wp[c], mod);
+    }
+    R->exact[3] = 0;
+    for(int c = 0; c < 4; c++) R->gcd_r2t[c] = J.gcd_given ? J.sc->gcd[c] : g[c];
+    if(J.metrics & QMIV_M_PSNR)   { for(int c = 0; c < 3; c++) R->psnr[c] = ps[c];   R->psnr[3] = 0;   R->psnr_pic = weighted3(ps, p.w_avg); }
+    if(J.metrics & QMIV_M_WSPSNR) { for(int c = 0; c < 3; c++) R->wspsnr[c] = wp[c]; R->wspsnr[3] = 0; R->wspsnr_pic = weighted3(wp, p.w_avg); }
+    __threadfence();
+    J.sc->stats_done = 0; // self-reset for the next use of this job slot
+  }
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kStatsThreads) k_stats(const DevJob* __restrict__ jobs, int njobs, Params p)
+{
+  __shared__ double scratch[2 * (kStatsThreads / 32)];
+  __shared__ bool is_last;
+  const int j = find_job<0>(jobs, njobs, blockIdx.x);
+  const DevJob& J = jobs[j];
+  const int y = 2 * (blockIdx.x - J.stat_base);
+
+  int sd[2][3] = { { 0, 0, 0 }, { 0, 0, 0 } };
+  unsigned long long ssd[2][3] = { { 0, 0, 0 }, { 0, 0, 0 } };
+  const bool vec = vec_ok(J);
+  if(J.sbytes == 1) stats_rowpair<uint8_t>(J, y, vec, sd, ssd);
+  else              stats_rowpair<uint16_t>(J, y, vec, sd, ssd);
+
+  // block reduction of 6 int sums and 6 64-bit sums
+  __shared__ int s_sd[kStatsThreads / 32][6];
+  __shared__ unsigned long long s_ssd[kStatsThreads / 32][6];
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  #pragma unroll
+  for(int r = 0; r < 2; r++)
+    #pragma unroll
+    for(int c = 0; c < 3; c++)
+    {
+      const int a = warp_sum(sd[r][c]);
+      const unsigned long long b = warp_sum(ssd[r][c]);
+      if(l == 0) { s_sd[w][r * 3 + c] = a; s_ssd[w][r * 3 + c] = b; }
+    }
+  __syncthreads();
+  if(threadIdx.x < 12)
+  {
+    const int r = threadIdx.x / 6, q = threadIdx.x % 6, c = q % 3;
+    const bool is_ssd = q >= 3;
+    int src_r = r;
+    long long mult = 1;
+    if(J.cshift && c > 0) { src_r = 0; mult = 2; } // chroma row counted 2x per luma row
+    long long v = 0;
+    for(int k = 0; k < kStatsThreads / 32; k++) v += is_ssd ? (long long)s_ssd[k][src_r * 3 + c] : (long long)s_sd[k][src_r * 3 + c];
+    if(y + r < J.H) J.stat_rows[(int64_t)(y + r) * 6 + q] = v * mult;
+  }
+  // zero this row pair's CPS accumulators for the CPS kernel that follows
+  if((J.metrics & (QMIV_M_IVPSNR | QMIV_M_IVSSIM)) && threadIdx.x >= 32 && threadIdx.x < 44)
+  {
+    const int t = threadIdx.x - 32, dir = t / 6, r = (t % 6) / 3, c = t % 3;
+    if(y + r < J.H) J.cps_rows[((int64_t)dir * J.H + y + r) * 3 + c] = 0ull;
+  }
+
+  __threadfence();
+  __syncthreads();
+  if(threadIdx.x == 0) is_last = atomicAdd(&J.sc->stats_done, 1u) == (unsigned)(J.stat_blocks - 1);
+  __syncthreads();
+  if(is_last)
+  {
+    __threadfence();
+    finalize_stats(J, p, scratch);
+  }
+}
+
+cudaError_t launch_stats(const DevJob* d_jobs, const DevJob* h_jobs, int n, const Params& p, cudaStream_t st)
+{
+  int blocks = 0;
+  for(int i = 0; i < n; i++) blocks = h_jobs[i].stat_base + h_jobs[i].stat_blocks;
+  if(blocks == 0) return cudaSuccess;
+  k_stats<<<blocks, kStatsThreads, 0, st>>>(d_jobs, n, p);
+  return cudaGetLastError();
+}
+
+}  // namespace qmiv

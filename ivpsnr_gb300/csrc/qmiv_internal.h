@@ -1,0 +1,66 @@
+// Internal device-side descriptors shared by the kernels and the host launcher.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/qmiv_gb300.h"
+
+namespace qmiv {
+
+constexpr int kMaxSR = 16;
+
+// Per-job scalars produced on the device and consumed by later kernels of the same job.
+struct JobScalars {
+  int32_t  gcd[4];          // GCD_R2T after the stats kernel (or supplied by the caller)
+  uint32_t stats_done;      // last-block counters (self-resetting)
+  uint32_t cps_done;
+  uint32_t ssim_done;
+  int32_t  status;
+  double   ssim_acc[8][3];  // SSIM plane sums for the current job: [pass][cmp] (see k_ssim)
+};
+
+// One picture pair as the kernels see it.
+struct DevJob {
+  const void* p0[3];
+  const void* p1[3];
+  int32_t stride0[3], stride1[3];
+  int32_t W, H, bd, sbytes, cshift;   // cshift 1: 4:2:0 chroma, 0: 4:4:4
+  uint32_t metrics;
+  int32_t use_ws;
+  const double* ws;                   // row weights (H) when use_ws
+  double ws_corr;                     // H / sum(w)
+  uint16_t* scp0[3];                  // built from picture 0 (T2R argmin), may be null
+  uint16_t* scp1[3];                  // built from picture 1 (R2T argmin), may be null
+  int32_t scp_stride;
+  int32_t gcd_given;                  // 1: sc->gcd preset by the host, stats kernel leaves it
+  int64_t* stat_rows;                 // [H][6]: sum(P1-P0)[3], sum((P1-P0)^2)[3]
+  unsigned long long* cps_rows;       // [2][H][3]: per-row CPS SSE, direction R2T then T2R
+  JobScalars* sc;
+  qmiv_frame_result* result;
+  // grid decomposition
+  int32_t stat_blocks, stat_base;     // row pairs
+  int32_t cps_strips, cps_segs, cps_seg_chunks, cps_base;
+};
+
+// Launch-wide parameters (the handle's options, pre-digested on the host).
+struct Params {
+  int32_t sr;
+  int32_t w_search[3];
+  int32_t w_avg[3];
+  int32_t maxdiff_for_bd[15][3];      // rne_f32(unc * Max) per bit depth (index bd) and component
+  int32_t fake_exact;
+  int32_t legacy_ws8;
+  // CPS key construction: E * M + k with (s*dY)^2 = M*w0*dY^2
+  uint32_t key_m;                     // M
+  int32_t key_m_log2;                 // log2(M) if M is a power of two, else -1
+  int32_t luma_scale;                 // s
+  int32_t luma_scale_log2;            // log2(s) if s is a power of two, else -1
+};
+
+// Host-side launchers (defined in the .cu files).
+cudaError_t launch_stats(const DevJob* d_jobs, const DevJob* h_jobs, int n, const Params& p, cudaStream_t st);
+cudaError_t launch_cps(const DevJob* d_jobs, const DevJob* h_jobs, int n, const Params& p, int variant, cudaStream_t st);
+int cps_variant_count();
+const char* cps_variant_name(int v);
+
+}  // namespace qmiv
