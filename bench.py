@@ -34,7 +34,12 @@ BD = 10
 WORKLOAD = "multiview-ivpsnr-wspsnr-10bit-420: 3x4096x2048 ERP + 6x1920x1080 + 3x2048x1088, 8 frames, SR 2"
 
 
-def jobs_list():
+SMALL = "small-profile-case: 24 pairs 1920x1080 10-bit 4:2:0 (150 MB), SR 2"
+
+
+def jobs_list(small=False):
+    if small:
+        return [(3, f, 1920, 1080, False) for f in range(24)]
     out = []
     for v, (w, h, erp) in enumerate(VIEWS):
         for f in range(FRAMES):
@@ -180,7 +185,7 @@ def run_ours(args):
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    jobs = jobs_list()
+    jobs = jobs_list(args.workload == "small")
     host = make_inputs(jobs)
     devbufs = []
     for (ref, tst) in host:
@@ -240,6 +245,12 @@ def run_ours(args):
     px_per_step = sum(w * h for (_, _, w, h, _) in jobs)
     value = px_per_step * world / (ms * 1e-3) / 1e9
 
+    if args.kernels_only:
+        if rank == 0:
+            print(json.dumps({"workload": SMALL if args.workload == "small" else WORKLOAD, "ms_per_step": ms,
+                              "value": value, "unit": "Gpixel/s"}))
+        P.close()
+        return
     # correctness spot check of the timed results against the oracle on one small view
     res_host.copy_(res_dev)
     r0 = _abi.FrameResult.from_buffer_copy(bytes(res_host[:rsz].numpy()))
@@ -346,6 +357,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="multiview", choices=["multiview", "small"],
+                    help="small: the 24-pair 1080p case used for ncu captures")
+    ap.add_argument("--kernels-only", action="store_true",
+                    help="time only the batched launches (for profiler captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

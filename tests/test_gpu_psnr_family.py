@@ -114,7 +114,7 @@ def test_every_cps_variant(gpu_lib, oq, variant):
     with gpu_lib.Processor(w, h, search_range=sr) as P:
         P.set_cps_variant(variant)
         gpu = P.calc_frame(gpu_lib.make_pic(_planes(ref, w, h), bd), gpu_lib.make_pic(_planes(tst, w, h), bd),
-                           gpu_lib.M_IVPSNR)
+                           gpu_lib.M_PSNR | gpu_lib.M_WSPSNR | gpu_lib.M_IVPSNR)
     _cmp(gpu, ora)
 
 
