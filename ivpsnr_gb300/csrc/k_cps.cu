@@ -20,14 +20,12 @@
 // roundup4(B) >= B pixels (apps/QMIV/src/xAppQMIV.cpp:330, xPixelOpsSTD.cpp:210).
 #include <climits>
 
-#include "qmiv_device.cuh"
+#include "qmiv_cps_common.cuh"
 
 namespace qmiv {
 
 namespace {
 
-__host__ __device__ constexpr int fdiv2(int v) { return v >= 0 ? v / 2 : -((-v + 1) / 2); } // floor(v/2)
-__host__ __device__ constexpr int ceil2(int v) { return (v + 1) / 2; }
 
 constexpr int kChunk = 64; // columns per chunk: 32 lanes x 2 columns
 
@@ -45,76 +43,6 @@ struct Geo {
   static constexpr int NT   = 2 * NWG * 32;                    // threads
 };
 
-// ------------------------------------------------------------------------------------
-// Last block of a job: IV-PSNR from the per-row CPS sums.
-// ------------------------------------------------------------------------------------
-__device__ void finalize_cps(const DevJob& J, const Params& p, double* scratch)
-{
-  __shared__ unsigned long long s_tot[2][3];
-  __shared__ double s_ws[2][3];
-  const int64_t area = (int64_t)J.W * J.H;
-  for(int d = 0; d < 2; d++)
-    for(int c = 0; c < 3; c++)
-    {
-      unsigned long long t = 0;
-      Kbns k = { 0.0, 0.0 };
-      for(int y = threadIdx.x; y < J.H; y += blockDim.x)
-      {
-        const unsigned long long v = __ldcg(J.cps_rows + ((int64_t)d * J.H + y) * 3 + c);
-        t += v;
-        if(J.use_ws) k = kbns_add(k, __dmul_rn((double)v, J.ws[y]));
-      }
-      t = warp_sum(t);
-      __syncthreads();
-      if((threadIdx.x & 31) == 0) scratch[threadIdx.x >> 5] = __longlong_as_double((long long)t);
-      __syncthreads();
-      if(threadIdx.x == 0)
-      {
-        unsigned long long a = 0;
-        for(int w = 0; w < (int)(blockDim.x >> 5); w++) a += (unsigned long long)__double_as_longlong(scratch[w]);
-        s_tot[d][c] = a;
-      }
-      __syncthreads();
-      if(J.use_ws) { const double r = block_kbns(k, scratch); if(threadIdx.x == 0) s_ws[d][c] = r; }
-    }
-  if(threadIdx.x == 0)
-  {
-    qmiv_frame_result* R = J.result;
-    double q[2];
-    for(int d = 0; d < 2; d++)
-    {
-      double qc[3];
-      for(int c = 0; c < 3; c++)
-      { // xIVPSNR.cpp:117-126: ERP uses the weighted sum without the H/sum(w) correction
-        const double e = J.use_ws ? s_ws[d][c] : (double)s_tot[d][c];
-        qc[c] = psnr_from_ssd(e > 0 ? e : 1.0, area, J.bd);
-      }
-      q[d] = weighted3(qc, p.w_avg);
-    }
-    for(int c = 0; c < 3; c++) { R->sse_r2t[c] = s_tot[0][c]; R->sse_t2r[c] = s_tot[1][c]; }
-    R->sse_r2t[3] = 0; R->sse_t2r[3] = 0;
-    if(J.metrics & QMIV_M_IVPSNR)
-    {
-      R->ivpsnr_r2t = q[0];
-      R->ivpsnr_t2r = q[1];
-      R->ivpsnr = q[1] < q[0] ? q[1] : q[0]; // std::min(R2T, T2R) (xIVPSNR.cpp:55)
-    }
-    __threadfence();
-    J.sc->cps_done = 0;
-  }
-}
-
-__device__ __forceinline__ bool cps_last_block(const DevJob& J)
-{
-  __shared__ bool is_last;
-  __threadfence();
-  __syncthreads();
-  if(threadIdx.x == 0) is_last = atomicAdd(&J.sc->cps_done, 1u) == (unsigned)(J.cps_strips * J.cps_segs - 1);
-  __syncthreads();
-  return is_last;
-}
-
-__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
 // ------------------------------------------------------------------------------------
 // Fast 4:2:0 kernel
@@ -383,21 +311,28 @@ __global__ void __launch_bounds__(kGenTX * kGenTY * 2) k_cps_generic(const DevJo
 // ------------------------------------------------------------------------------------
 // Variant table
 // ------------------------------------------------------------------------------------
-using KernelFn = void (*)(const DevJob*, int, Params);
-struct Variant { const char* name; KernelFn fn; int threads; int sr; int rows; bool key64; };
+template <int SR, int RPT, int NWG, typename KT>
+cudaError_t launch420(const DevJob* d, int n, int blocks, const Params& p, cudaStream_t st)
+{
+  k_cps420<SR, RPT, NWG, KT><<<blocks, Geo<SR, RPT, NWG>::NT, 0, st>>>(d, n, p);
+  return cudaGetLastError();
+}
+cudaError_t launch_generic(const DevJob* d, int n, int blocks, const Params& p, cudaStream_t st)
+{
+  k_cps_generic<<<blocks, kGenTX * kGenTY * 2, 0, st>>>(d, n, p);
+  return cudaGetLastError();
+}
 
-#define V420(SR, RPT, NWG, KT, K64, SUF) { "cps420_sr" #SR "_rpt" #RPT "_nwg" #NWG SUF, \
-                                           k_cps420<SR, RPT, NWG, KT>, Geo<SR, RPT, NWG>::NT, SR, RPT * NWG, K64 }
-const Variant kVariants[] = {
-  { "cps_generic", k_cps_generic, kGenTX * kGenTY * 2, 0, kGenTY, true },
+#define V420(SR, RPT, NWG, KT, K64, SUF) { "cps420_sr" #SR "_rpt" #RPT "_nwg" #NWG SUF, launch420<SR, RPT, NWG, KT>, \
+                                           SR, RPT * NWG, 64, K64, 1, 0 }
+const CpsVariant kVariants[] = {
+  { "cps_generic", launch_generic, 0, kGenTY, kGenTX, true, 0, 0 },
   V420(1, 8, 2, unsigned int, false, "_k32"),
   V420(2, 8, 2, unsigned int, false, "_k32"),
   V420(2, 4, 2, unsigned int, false, "_k32"),
-  V420(2, 8, 1, unsigned int, false, "_k32"),
   V420(2, 4, 4, unsigned int, false, "_k32"),
   V420(3, 8, 2, unsigned int, false, "_k32"),
   V420(4, 8, 2, unsigned int, false, "_k32"),
-  V420(4, 4, 2, unsigned int, false, "_k32"),
   V420(1, 8, 2, unsigned long long, true, "_k64"),
   V420(2, 8, 2, unsigned long long, true, "_k64"),
   V420(3, 8, 2, unsigned long long, true, "_k64"),
@@ -407,20 +342,10 @@ const Variant kVariants[] = {
 
 }  // namespace
 
-int cps_variant_count() { return (int)(sizeof(kVariants) / sizeof(kVariants[0])); }
-const char* cps_variant_name(int v) { return (v >= 0 && v < cps_variant_count()) ? kVariants[v].name : ""; }
-int cps_variant_sr(int v) { return kVariants[v].sr; }
-int cps_variant_rows(int v) { return kVariants[v].rows; }
-bool cps_variant_key64(int v) { return kVariants[v].key64; }
-
-cudaError_t launch_cps(const DevJob* d_jobs, const DevJob* h_jobs, int n, const Params& p, int variant, cudaStream_t st)
+const CpsVariant* cps_variants_staged(int* n)
 {
-  if(variant < 0 || variant >= cps_variant_count()) return cudaErrorInvalidValue;
-  int blocks = 0;
-  for(int i = 0; i < n; i++) blocks = h_jobs[i].cps_base + h_jobs[i].cps_strips * h_jobs[i].cps_segs;
-  if(blocks == 0) return cudaSuccess;
-  kVariants[variant].fn<<<blocks, kVariants[variant].threads, 0, st>>>(d_jobs, n, p);
-  return cudaGetLastError();
+  *n = (int)(sizeof(kVariants) / sizeof(kVariants[0]));
+  return kVariants;
 }
 
 }  // namespace qmiv

@@ -138,6 +138,8 @@ __device__ void finalize_stats(const DevJob& J, const Params& p, double* scratch
       g[c] = v < -md ? -md : (v > md ? md : v);
     }
     if(!J.gcd_given) { for(int c = 0; c < 4; c++) J.sc->gcd[c] = g[c]; }
+    J.sc->status = 0;
+    R->status = 0;
     double ps[3], wp[3];
     const double fake = psnr_from_ssd(1.0, area, J.bd);
     for(int c = 0; c < 3; c++)

@@ -10,19 +10,46 @@
 #include <string>
 #include <vector>
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "qmiv_internal.h"
 
-namespace qmiv {
-int cps_variant_sr(int v);
-int cps_variant_rows(int v);
-bool cps_variant_key64(int v);
-}  // namespace qmiv
-
 using namespace qmiv;
 
 namespace {
+
+// All compiled CPS variants: index 0 is the generic kernel.
+const std::vector<CpsVariant>& variants()
+{
+  static std::vector<CpsVariant> v = [] {
+    std::vector<CpsVariant> out;
+    int n = 0;
+    const CpsVariant* a = cps_variants_staged(&n);
+    out.insert(out.end(), a, a + n);
+    a = cps_variants_tma(&n);
+    out.insert(out.end(), a, a + n);
+    return out;
+  }();
+  return v;
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn()
+{
+  static EncodeTiledFn fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+       q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return (EncodeTiledFn)f;
+  }();
+  return fn;
+}
 
 thread_local std::string g_last_error;
 
@@ -40,11 +67,14 @@ qmiv_status fail(qmiv_status s, const char* fmt, ...)
     if(e_ != cudaSuccess) return fail(QMIV_CUDA_ERROR, "%s: %s", #expr, cudaGetErrorString(e_)); \
   } while(0)
 
-// Device slot for one job: scratch rows and scalars.
+// Device slot for one job: scratch rows and scalars, plus the tensor maps of its planes.
 struct Slot {
   int64_t* stat_rows = nullptr;          // [max_h][6]
   unsigned long long* cps_rows = nullptr; // [2][max_h][3]
   JobScalars* sc = nullptr;
+  void* d_tmaps = nullptr;               // 6 x 128 B in device memory
+  uint64_t tmap_key[16] = { 0 };         // what the maps were encoded for
+  bool tmap_valid = false;
 };
 
 struct SeqAcc { std::vector<double> v[16]; };
@@ -123,20 +153,39 @@ bool key32_ok(const qmiv_handle* h, int bd)
   return kmax < (1ull << 32) && (uint64_t)p.luma_scale * D < 46340ull;
 }
 
+// Can the TMA kernels stage this job? 16-byte aligned planes and row pitches.
+bool tma_ok(const DevJob& j)
+{
+  if(!j.cshift || !encode_fn()) return false;
+  for(int c = 0; c < 3; c++)
+  {
+    if((((uintptr_t)j.p0[c]) | ((uintptr_t)j.p1[c])) & 15) return false;
+    if(((j.stride0[c] * j.sbytes) | (j.stride1[c] * j.sbytes)) & 15) return false;
+  }
+  return true;
+}
+
 int pick_cps_variant(const qmiv_handle* h, const DevJob& j)
 {
+  const auto& V = variants();
   const int sr = h->params.sr;
   if(!j.cshift || h->opt.cmp_w_search[0] < 1 || sr < 1 || sr > 4) return 0; // generic
   if(h->cps_variant_override == 0) return 0;
   const bool k64 = !key32_ok(h, j.bd);
-  if(h->cps_variant_override > 0)
-  {
-    const int v = h->cps_variant_override;
-    if(cps_variant_sr(v) == sr && cps_variant_key64(v) == k64) return v;
-  }
-  for(int v = 1; v < cps_variant_count(); v++)
-    if(cps_variant_sr(v) == sr && cps_variant_key64(v) == k64 && cps_variant_rows(v) == 16 &&
-       std::strstr(cps_variant_name(v), "rpt8_nwg2")) return v;
+  const bool tma = tma_ok(j);
+  auto fits = [&](int v) {
+    const CpsVariant& c = V[v];
+    if(c.sr != sr || c.key64 != k64) return false;
+    if(c.kind == 2 && (!tma || c.sbytes != j.sbytes)) return false;
+    return c.kind != 0;
+  };
+  if(h->cps_variant_override > 0 && h->cps_variant_override < (int)V.size() && fits(h->cps_variant_override))
+    return h->cps_variant_override;
+  // default: the TMA kernel with 32-row strips and 8 warps, else the staged-load kernel
+  for(int v = 1; v < (int)V.size(); v++)
+    if(fits(v) && V[v].kind == 2 && V[v].rows == 32 && std::strstr(V[v].name, "_q4_w4")) return v;
+  for(int v = 1; v < (int)V.size(); v++)
+    if(fits(v) && V[v].kind == 1 && std::strstr(V[v].name, "rpt8_nwg2")) return v;
   return 0;
 }
 
@@ -230,7 +279,7 @@ void plan_grid(qmiv_handle* h, DevJob* jobs, int n, const std::vector<int>& vari
     j.stat_blocks = (j.H + 1) / 2;
     j.stat_base = sbase;
     sbase += j.stat_blocks;
-    const int rows = cps_variant_rows(variant[i]);
+    const int rows = variants()[variant[i]].rows;
     j.cps_strips = (j.H + rows - 1) / rows;
     strips_total += j.cps_strips;
   }
@@ -298,6 +347,48 @@ cudaError_t prof_mark(qmiv_handle* h, const char* name, cudaStream_t st, bool be
   return cudaEventRecord(h->prof[h->prof_n++].b, st);
 }
 
+// Encode (or reuse) the six tensor maps a TMA variant reads for one job's planes.
+qmiv_status ensure_tmaps(qmiv_handle* h, int slot, DevJob& j, const CpsVariant& v, cudaStream_t st)
+{
+  Slot& S = h->slots[slot];
+  const int sb = j.sbytes, XA = 16 / sb, R = v.rows, SR = v.sr, CS = (SR + 1) / 2;
+  const int fd = (R - 1 + SR) >= 0 ? (R - 1 + SR) / 2 : -((-(R - 1 + SR) + 1) / 2);
+  const uint32_t RW = 64 + 2 * XA, TH = R + 2 * SR, CRW = 32 + 2 * XA, CTH = fd + CS + 1;
+  uint64_t key[16] = { 0 };
+  for(int c = 0; c < 3; c++)
+  {
+    key[c] = (uint64_t)(uintptr_t)j.p0[c]; key[3 + c] = (uint64_t)(uintptr_t)j.p1[c];
+    key[6 + c] = ((uint64_t)(uint32_t)j.stride0[c] << 32) | (uint32_t)j.stride1[c];
+  }
+  key[9] = ((uint64_t)(uint32_t)j.W << 32) | (uint32_t)j.H;
+  key[10] = ((uint64_t)RW << 48) | ((uint64_t)TH << 32) | ((uint64_t)CRW << 16) | CTH;
+  key[11] = (uint64_t)sb;
+  j.tmaps = S.d_tmaps;
+  if(S.tmap_valid && std::memcmp(key, S.tmap_key, sizeof(key)) == 0) return QMIV_OK;
+  EncodeTiledFn enc = encode_fn();
+  if(!enc) return fail(QMIV_CUDA_ERROR, "cuTensorMapEncodeTiled unavailable");
+  alignas(64) CUtensorMap maps[6];
+  for(int pic = 0; pic < 2; pic++)
+    for(int c = 0; c < 3; c++)
+    {
+      const void* base = pic == 0 ? j.p0[c] : j.p1[c];
+      const int stride = pic == 0 ? j.stride0[c] : j.stride1[c];
+      const cuuint64_t dims[2] = { (cuuint64_t)(c ? j.W / 2 : j.W), (cuuint64_t)(c ? j.H / 2 : j.H) };
+      const cuuint64_t strides[1] = { (cuuint64_t)stride * sb };
+      const cuuint32_t box[2] = { c ? CRW : RW, c ? CTH : TH };
+      const cuuint32_t estr[2] = { 1, 1 };
+      CUresult r = enc(&maps[pic * 3 + c], sb == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 2,
+                       const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                       CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if(r != CUDA_SUCCESS) { S.tmap_valid = false; return fail(QMIV_CUDA_ERROR, "cuTensorMapEncodeTiled failed (%d)", (int)r); }
+    }
+  CUDA_TRY(cudaMemcpyAsync(S.d_tmaps, maps, sizeof(maps), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaStreamSynchronize(st)); // `maps` lives on this stack frame
+  std::memcpy(S.tmap_key, key, sizeof(key));
+  S.tmap_valid = true;
+  return QMIV_OK;
+}
+
 // Run stats + CPS for n jobs already in h->h_jobs[0..n) (slots 0..n).
 qmiv_status run_psnr_family(qmiv_handle* h, int n, cudaStream_t st)
 {
@@ -321,6 +412,14 @@ qmiv_status run_psnr_family(qmiv_handle* h, int n, cudaStream_t st)
     for(int i = first; i <= last; i++) { sorted[i].cps_base = base; base += (var[order[i]] < 0) ? 0 : sorted[i].cps_strips * sorted[i].cps_segs; }
     first = last + 1;
   }
+  for(int i = 0; i < n; i++)
+  {
+    if(var[order[i]] > 0 && variants()[var[order[i]]].kind == 2)
+    {
+      qmiv_status ts = ensure_tmaps(h, order[i], sorted[i], variants()[var[order[i]]], st);
+      if(ts != QMIV_OK) return ts;
+    }
+  }
   std::memcpy(h->h_jobs, sorted.data(), sizeof(DevJob) * n);
   CUDA_TRY(cudaMemcpyAsync(h->d_jobs, h->h_jobs, sizeof(DevJob) * n, cudaMemcpyHostToDevice, st));
   h->prof_n = 0;
@@ -335,8 +434,11 @@ qmiv_status run_psnr_family(qmiv_handle* h, int n, cudaStream_t st)
     while(last + 1 < n && var[order[last + 1]] == var[order[first]]) last++;
     if(var[order[first]] >= 0)
     {
-      CUDA_TRY(prof_mark(h, cps_variant_name(var[order[first]]), st, true));
-      CUDA_TRY(launch_cps(h->d_jobs + first, h->h_jobs + first, last - first + 1, h->params, var[order[first]], st));
+      const CpsVariant& cv = variants()[var[order[first]]];
+      int blocks = 0;
+      for(int i = first; i <= last; i++) blocks = h->h_jobs[i].cps_base + h->h_jobs[i].cps_strips * h->h_jobs[i].cps_segs;
+      CUDA_TRY(prof_mark(h, cv.name, st, true));
+      if(blocks > 0) CUDA_TRY(cv.launch(h->d_jobs + first, last - first + 1, blocks, h->params, st));
       CUDA_TRY(prof_mark(h, nullptr, st, false));
       h->launches++;
     }
@@ -421,7 +523,8 @@ qmiv_status qmiv_create(qmiv_handle** out, const qmiv_options* opt, int32_t max_
   const size_t rows_b = (size_t)max_h * 6 * sizeof(int64_t);
   const size_t cps_b = (size_t)2 * max_h * 3 * sizeof(unsigned long long);
   const size_t sc_b = (sizeof(JobScalars) + 255) & ~(size_t)255;
-  const size_t per = ((rows_b + 255) & ~(size_t)255) + ((cps_b + 255) & ~(size_t)255) + sc_b;
+  const size_t tm_b = 6 * 128;
+  const size_t per = ((rows_b + 255) & ~(size_t)255) + ((cps_b + 255) & ~(size_t)255) + sc_b + tm_b;
   if(cudaMalloc(&h->slot_mem, per * max_jobs) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "slot scratch %zu B", per * max_jobs));
   if(cudaMemset(h->slot_mem, 0, per * max_jobs) != cudaSuccess) return cleanup(fail(QMIV_CUDA_ERROR, "memset"));
   h->slots.resize(max_jobs);
@@ -430,7 +533,8 @@ qmiv_status qmiv_create(qmiv_handle** out, const qmiv_options* opt, int32_t max_
     uint8_t* b = (uint8_t*)h->slot_mem + per * i;
     h->slots[i].stat_rows = (int64_t*)b; b += (rows_b + 255) & ~(size_t)255;
     h->slots[i].cps_rows = (unsigned long long*)b; b += (cps_b + 255) & ~(size_t)255;
-    h->slots[i].sc = (JobScalars*)b;
+    h->slots[i].sc = (JobScalars*)b; b += sc_b;
+    h->slots[i].d_tmaps = b;
   }
   if(cudaMalloc(&h->d_jobs, sizeof(DevJob) * max_jobs) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "job table"));
   if(cudaMallocHost(&h->h_jobs, sizeof(DevJob) * max_jobs) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "pinned job table"));
@@ -475,8 +579,8 @@ qmiv_status qmiv_set_options(qmiv_handle* h, const qmiv_options* opt)
 
 int64_t qmiv_kernel_launches(const qmiv_handle* h) { return h ? h->launches : 0; }
 
-int32_t qmiv_cps_variant_count(void) { return cps_variant_count(); }
-const char* qmiv_cps_variant_name(int32_t v) { return cps_variant_name(v); }
+int32_t qmiv_cps_variant_count(void) { return (int32_t)variants().size(); }
+const char* qmiv_cps_variant_name(int32_t v) { return (v >= 0 && v < (int32_t)variants().size()) ? variants()[v].name : ""; }
 qmiv_status qmiv_set_profiling(qmiv_handle* h, int32_t enable)
 {
   if(!h) return fail(QMIV_BAD_ARG, "handle is null");
@@ -503,7 +607,7 @@ int32_t qmiv_kernel_times(qmiv_handle* h, const char** names, double* ms, int32_
 qmiv_status qmiv_set_cps_variant(qmiv_handle* h, int32_t v)
 {
   if(!h) return fail(QMIV_BAD_ARG, "handle is null");
-  if(v < -1 || v >= cps_variant_count()) return fail(QMIV_BAD_ARG, "variant %d", v);
+  if(v < -1 || v >= (int32_t)variants().size()) return fail(QMIV_BAD_ARG, "variant %d", v);
   h->cps_variant_override = v;
   return QMIV_OK;
 }

@@ -33,6 +33,7 @@ struct DevJob {
   uint16_t* scp1[3];                  // built from picture 1 (R2T argmin), may be null
   int32_t scp_stride;
   int32_t gcd_given;                  // 1: sc->gcd preset by the host, stats kernel leaves it
+  const void* tmaps;                  // 6 tensor maps (picture 0 Y,Cb,Cr then picture 1) or null
   int64_t* stat_rows;                 // [H][6]: sum(P1-P0)[3], sum((P1-P0)^2)[3]
   unsigned long long* cps_rows;       // [2][H][3]: per-row CPS SSE, direction R2T then T2R
   JobScalars* sc;
@@ -59,8 +60,19 @@ struct Params {
 
 // Host-side launchers (defined in the .cu files).
 cudaError_t launch_stats(const DevJob* d_jobs, const DevJob* h_jobs, int n, const Params& p, cudaStream_t st);
-cudaError_t launch_cps(const DevJob* d_jobs, const DevJob* h_jobs, int n, const Params& p, int variant, cudaStream_t st);
-int cps_variant_count();
-const char* cps_variant_name(int v);
+
+// One compiled form of the CPS kernel.
+struct CpsVariant {
+  const char* name;
+  cudaError_t (*launch)(const DevJob* d_jobs, int n, int blocks, const Params& p, cudaStream_t st);
+  int sr;        // search range it is specialised for (0: any)
+  int rows;      // strip rows per block (generic: tile rows)
+  int cols;      // columns per chunk (generic: tile columns)
+  bool key64;    // 64-bit packed keys (high bit depths)
+  int kind;      // 0 generic, 1 staged loads, 2 TMA double-buffered
+  int sbytes;    // sample size it requires (0: any)
+};
+const CpsVariant* cps_variants_staged(int* n);  // k_cps.cu
+const CpsVariant* cps_variants_tma(int* n);     // k_cps_tma.cu
 
 }  // namespace qmiv

@@ -108,14 +108,21 @@ def test_every_cps_variant(gpu_lib, oq, variant):
         pytest.skip("no such variant")
     name = names[variant]
     sr = 2 if variant == 0 else int(name.split("_sr")[1].split("_")[0])
-    w, h, bd = 300, 90, 12 if name.endswith("k64") else 10
+    bd = 12 if "k64" in name else (8 if name.endswith("_u8") else 10)
+    dtype = np.uint8 if bd == 8 else np.uint16
+    # 352 x 98: not multiples of the chunk or strip; rows of 16-byte multiples in 8 and 16 bits
+    w, h = 352, 98
     ref, tst = _case(w, h, bd, 31 + variant)
     ora, _, _ = _oracle(oq, ref, tst, w, h, bd, search_range=sr)
     with gpu_lib.Processor(w, h, search_range=sr) as P:
         P.set_cps_variant(variant)
-        gpu = P.calc_frame(gpu_lib.make_pic(_planes(ref, w, h), bd), gpu_lib.make_pic(_planes(tst, w, h), bd),
+        P.set_profiling(True)
+        gpu = P.calc_frame(gpu_lib.make_pic(_planes(ref, w, h, dtype), bd), gpu_lib.make_pic(_planes(tst, w, h, dtype), bd),
                            gpu_lib.M_PSNR | gpu_lib.M_WSPSNR | gpu_lib.M_IVPSNR)
+        ran = [n for n, _ in P.kernel_times()]
+    assert name in ran, (name, ran)  # the requested variant is the one that ran
     _cmp(gpu, ora)
+    assert gpu["status"] == 0
 
 
 def test_scp_bit_exact(gpu_lib, oq):
