@@ -1,0 +1,95 @@
+"""Regenerates tests/golden/cases.json from the reference itself.
+
+Inputs are the deterministic synthetic pictures of ivpsnr_gb300.synth (their bytes are
+pinned by an md5 per case, so any machine can regenerate them); the expected values come
+from the reference's metric library built from its own sources by oracle/build_ref.sh and
+driven by oracle/ref_harness.cpp. Run on a machine that has the reference sources:
+
+    oracle/build_ref.sh && python tests/golden/make_golden.py
+"""
+import hashlib
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+from ivpsnr_gb300 import synth  # noqa: E402
+
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "qmiv_ref_harness")
+
+# name, w, h, bd, seed, generator kwargs, harness options
+CASES = [
+    # 8-bit widths avoid 64 (mod 128): there the reference's AVX-512 8-bit chroma upsample stores
+    # nothing (libs/pmbb-core/src/xPixelOpsAVX512.cpp:293, a shift by 64 in its tail mask)
+    ("cfg0_like_8bit_96x48", 96, 48, 8, synth.seed_for(0, 0, 0), {}, {}),
+    ("8bit_130x66", 130, 66, 8, 5, {}, {}),
+    ("10bit_holes_128x96", 128, 96, 10, 123, {"holes": True}, {}),
+    ("10bit_erp_256x128", 256, 128, 10, 77, {"holes": True}, {"erp": True}),
+    ("10bit_erp_lat90_128x64", 128, 64, 10, 78, {}, {"erp": True, "lat": 90}),
+    ("10bit_sr1_66x34", 66, 34, 10, 6, {}, {"sr": 1}),
+    ("10bit_sr3_100x50", 100, 50, 10, 7, {}, {"sr": 3}),
+    ("10bit_sr4_96x64", 96, 64, 10, 8, {}, {"sr": 4}),
+    ("12bit_96x64", 96, 64, 12, 9, {}, {}),
+    ("14bit_64x48", 64, 48, 14, 10, {}, {}),
+    ("8bit_tiny_6x4", 6, 4, 8, 12, {}, {}),
+    ("8bit_2x2", 2, 2, 8, 11, {}, {}),
+    ("10bit_noiseless_64x64", 64, 64, 10, 13, {"noise_sigma": 0.0, "offset": (0.0, 0.0, 0.0)}, {}),
+    ("10bit_bigoffset_80x40", 80, 40, 10, 14, {"offset": (9.0, -9.0, 6.0)}, {}),
+    ("cfg0_1920x1080_8bit", 1920, 1080, 8, synth.seed_for(0, 0, 0), {}, {}),
+    ("cfg1_view3_1920x1080_10bit", 1920, 1080, 10, synth.seed_for(1, 3, 0), {"holes": True}, {}),
+]
+
+
+def md5(*arrays):
+    h = hashlib.md5()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def run_case(name, w, h, bd, seed, gkw, hopt, tmp):
+    ref, tst = synth.pair420(w, h, bd, seed=seed, **gkw)
+    a, b = os.path.join(tmp, "a.yuv"), os.path.join(tmp, "b.yuv")
+    if bd == 8:
+        ref.astype(np.uint8).tofile(a)
+        tst.astype(np.uint8).tofile(b)
+    else:
+        ref.tofile(a)
+        tst.tofile(b)
+    cmd = [HARNESS, "-w", str(w), "-h", str(h), "-bd", str(bd), "-cf", "420", "-i0", a, "-i1", b, "-nth", "2",
+           "-dump", os.path.join(tmp, "d")]
+    if hopt.get("erp"):
+        cmd += ["-erp", "-lat", str(hopt.get("lat", 180))]
+    if "sr" in hopt:
+        cmd += ["-sr", str(hopt["sr"])]
+    if w < 16 or h < 16:  # the reference's MS-SSIM pyramid needs 4 halvings of at least 1 pixel
+        cmd += ["-ssim", "0"]
+    out = json.loads(subprocess.check_output(cmd).decode().splitlines()[0])
+    cps = np.fromfile(os.path.join(tmp, "d_f0_cps.bin"), np.int8)
+    scp = np.fromfile(os.path.join(tmp, "d_f0_scp.bin"), np.uint16)
+    out.pop("frame", None)
+    return {
+        "name": name, "w": w, "h": h, "bd": bd, "seed": seed, "gen": {k: list(v) if isinstance(v, tuple) else v for k, v in gkw.items()},
+        "opts": hopt, "input_md5": md5(ref, tst), "cps_md5": md5(cps), "scp_md5": md5(scp), "expected": out,
+    }
+
+
+def main():
+    if not os.path.exists(HARNESS):
+        sys.exit("build the reference first: oracle/build_ref.sh")
+    tmp = tempfile.mkdtemp()
+    cases = [run_case(*c, tmp) for c in CASES]
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "cases.json")
+    with open(path, "w") as f:
+        json.dump({"generator": "ivpsnr_gb300.synth.pair420", "reference": "pmbb-ivqm via oracle/ref_harness.cpp",
+                   "cases": cases}, f, indent=1)
+    print("wrote", path, len(cases), "cases")
+
+
+if __name__ == "__main__":
+    main()

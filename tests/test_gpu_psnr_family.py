@@ -108,7 +108,8 @@ def test_every_cps_variant(gpu_lib, oq, variant):
         pytest.skip("no such variant")
     name = names[variant]
     sr = 2 if variant == 0 else int(name.split("_sr")[1].split("_")[0])
-    bd = 12 if "k64" in name else (8 if name.endswith("_u8") else 10)
+    # 14-bit samples need 64-bit keys at every search range; 8-bit variants read uint8 planes
+    bd = 14 if "k64" in name else (8 if name.endswith("_u8") else 10)
     dtype = np.uint8 if bd == 8 else np.uint16
     # 352 x 98: not multiples of the chunk or strip; rows of 16-byte multiples in 8 and 16 bits
     w, h = 352, 98
