@@ -78,6 +78,7 @@ k_cps420_tma(const DevJob* __restrict__ jobs, int njobs, Params p)
   const int gs = dir == 0 ? 1 : -1;
   const int gd0 = gs * J.sc->gcd[0], gd1 = gs * J.sc->gcd[1], gd2 = gs * J.sc->gcd[2];
   const int s = p.luma_scale;
+  const unsigned one = p.one;
   const KeyT Mw1 = (KeyT)p.key_m * (KeyT)p.w_search[1];
   const KeyT Mw2 = (KeyT)p.key_m * (KeyT)p.w_search[2];
   const int mx = (1 << J.bd) - 1;
@@ -220,7 +221,9 @@ k_cps420_tma(const DevJob* __restrict__ jobs, int njobs, Params p)
                 const int jc = fdiv2(px + dx) + G::CS;
                 const int dd = tY[a][px] - r[px + dx + SR];
                 KeyT key;
-                if(sizeof(KeyT) == 4) key = (KeyT)(unsigned)(dd * dd) + (B[jr][jc] + (KeyT)k);
+                // the ALU pipe carries the difference and the min; the index add and the
+                // square go to the multiply-add pipe, so both pipes share the candidate loop
+                if(sizeof(KeyT) == 4) key = (KeyT)(unsigned)(dd * dd) + (KeyT)ptx::mad_u32((unsigned)B[jr][jc], one, (unsigned)k);
                 else                  key = (KeyT)((long long)dd * dd) + (B[jr][jc] + (KeyT)k);
                 best[a][px] = min(best[a][px], key);
               }

@@ -17,20 +17,22 @@ namespace qmiv {
 namespace {
 
 constexpr int kStatsThreads = 256;
+constexpr int kRowPairsPerBlock = kStatsThreads / 32; // one warp per pair of luma rows
 
-// sum(a-b) and sum((a-b)^2) over n samples of two rows
+// sum(a-b) and sum((a-b)^2) over n samples of two rows, one warp, 16-byte loads when aligned
 template <typename T>
-__device__ __forceinline__ void row_stats(const T* __restrict__ a, const T* __restrict__ b, int n, bool vec,
+__device__ __forceinline__ void row_stats(const T* __restrict__ a, const T* __restrict__ b, int n, bool vec, int lane,
                                           int& sd, unsigned long long& ssd)
 {
   int i0 = 0;
   if(vec)
-  { // 16-byte loads: 8 uint16 or 16 uint8 samples per load
+  {
     constexpr int V = 16 / sizeof(T);
     const int nv = n / V;
     const uint4* av = reinterpret_cast<const uint4*>(a);
     const uint4* bv = reinterpret_cast<const uint4*>(b);
-    for(int i = threadIdx.x; i < nv; i += blockDim.x)
+    #pragma unroll 4
+    for(int i = lane; i < nv; i += 32)
     {
       const uint4 x = __ldg(av + i), y = __ldg(bv + i);
       const T* xs = reinterpret_cast<const T*>(&x);
@@ -42,7 +44,7 @@ __device__ __forceinline__ void row_stats(const T* __restrict__ a, const T* __re
     }
     i0 = nv * V;
   }
-  for(int i = i0 + threadIdx.x; i < n; i += blockDim.x)
+  for(int i = i0 + lane; i < n; i += 32)
   {
     const int d = (int)a[i] - (int)b[i];
     sd += d; ssd += (unsigned long long)(d * d);
@@ -50,20 +52,20 @@ __device__ __forceinline__ void row_stats(const T* __restrict__ a, const T* __re
 }
 
 template <typename T>
-__device__ void stats_rowpair(const DevJob& J, int y, bool vec, int sd[2][3], unsigned long long ssd[2][3])
+__device__ void stats_rowpair(const DevJob& J, int y, bool vec, int lane, int sd[2][3], unsigned long long ssd[2][3])
 {
   const T* p0[3]; const T* p1[3];
   for(int c = 0; c < 3; c++) { p0[c] = (const T*)J.p0[c]; p1[c] = (const T*)J.p1[c]; }
   for(int r = 0; r < 2; r++)
   {
     if(y + r >= J.H) break;
-    row_stats<T>(p1[0] + (int64_t)(y + r) * J.stride1[0], p0[0] + (int64_t)(y + r) * J.stride0[0], J.W, vec, sd[r][0], ssd[r][0]);
+    row_stats<T>(p1[0] + (int64_t)(y + r) * J.stride1[0], p0[0] + (int64_t)(y + r) * J.stride0[0], J.W, vec, lane, sd[r][0], ssd[r][0]);
   }
   if(J.cshift)
   { // one chroma row serves luma rows y and y+1
     const int cy = y >> 1, cw = J.W >> 1;
     for(int c = 1; c < 3; c++)
-      row_stats<T>(p1[c] + (int64_t)cy * J.stride1[c], p0[c] + (int64_t)cy * J.stride0[c], cw, vec, sd[0][c], ssd[0][c]);
+      row_stats<T>(p1[c] + (int64_t)cy * J.stride1[c], p0[c] + (int64_t)cy * J.stride0[c], cw, vec, lane, sd[0][c], ssd[0][c]);
   }
   else
   {
@@ -71,7 +73,7 @@ __device__ void stats_rowpair(const DevJob& J, int y, bool vec, int sd[2][3], un
     {
       if(y + r >= J.H) break;
       for(int c = 1; c < 3; c++)
-        row_stats<T>(p1[c] + (int64_t)(y + r) * J.stride1[c], p0[c] + (int64_t)(y + r) * J.stride0[c], J.W, vec, sd[r][c], ssd[r][c]);
+        row_stats<T>(p1[c] + (int64_t)(y + r) * J.stride1[c], p0[c] + (int64_t)(y + r) * J.stride0[c], J.W, vec, lane, sd[r][c], ssd[r][c]);
     }
   }
 }
@@ -174,44 +176,44 @@ __global__ void __launch_bounds__(kStatsThreads) k_stats(const DevJob* __restric
   __shared__ bool is_last;
   const int j = find_job<0>(jobs, njobs, blockIdx.x);
   const DevJob& J = jobs[j];
-  const int y = 2 * (blockIdx.x - J.stat_base);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int y = 2 * ((blockIdx.x - J.stat_base) * kRowPairsPerBlock + w);
 
-  int sd[2][3] = { { 0, 0, 0 }, { 0, 0, 0 } };
-  unsigned long long ssd[2][3] = { { 0, 0, 0 }, { 0, 0, 0 } };
-  const bool vec = vec_ok(J);
-  if(J.sbytes == 1) stats_rowpair<uint8_t>(J, y, vec, sd, ssd);
-  else              stats_rowpair<uint16_t>(J, y, vec, sd, ssd);
-
-  // block reduction of 6 int sums and 6 64-bit sums
-  __shared__ int s_sd[kStatsThreads / 32][6];
-  __shared__ unsigned long long s_ssd[kStatsThreads / 32][6];
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  #pragma unroll
-  for(int r = 0; r < 2; r++)
+  if(y < J.H)
+  {
+    int sd[2][3] = { { 0, 0, 0 }, { 0, 0, 0 } };
+    unsigned long long ssd[2][3] = { { 0, 0, 0 }, { 0, 0, 0 } };
+    const bool vec = vec_ok(J);
+    if(J.sbytes == 1) stats_rowpair<uint8_t>(J, y, vec, lane, sd, ssd);
+    else              stats_rowpair<uint16_t>(J, y, vec, lane, sd, ssd);
+    long long v[2][6];
     #pragma unroll
-    for(int c = 0; c < 3; c++)
-    {
-      const int a = warp_sum(sd[r][c]);
-      const unsigned long long b = warp_sum(ssd[r][c]);
-      if(l == 0) { s_sd[w][r * 3 + c] = a; s_ssd[w][r * 3 + c] = b; }
+    for(int r = 0; r < 2; r++)
+      #pragma unroll
+      for(int c = 0; c < 3; c++)
+      {
+        v[r][c] = (long long)__reduce_add_sync(0xffffffffu, (unsigned)sd[r][c]);
+        v[r][c] = (long long)(int)v[r][c];
+        v[r][3 + c] = (long long)warp_sum(ssd[r][c]);
+      }
+    if(lane < 12)
+    { // lane = r*6 + q: rows y, y+1; q: sd[3], ssd[3]; a chroma row counts 2x per luma row (4:2:0)
+      const int r = lane / 6, q = lane % 6, c = q % 3;
+      const bool chroma420 = J.cshift && c > 0;
+      long long val = 0;
+      #pragma unroll
+      for(int rr = 0; rr < 2; rr++)
+        #pragma unroll
+        for(int qq = 0; qq < 6; qq++)
+          if(qq == q && rr == (chroma420 ? 0 : r)) val = v[rr][qq];
+      if(y + r < J.H) J.stat_rows[(int64_t)(y + r) * 6 + q] = chroma420 ? 2 * val : val;
     }
-  __syncthreads();
-  if(threadIdx.x < 12)
-  {
-    const int r = threadIdx.x / 6, q = threadIdx.x % 6, c = q % 3;
-    const bool is_ssd = q >= 3;
-    int src_r = r;
-    long long mult = 1;
-    if(J.cshift && c > 0) { src_r = 0; mult = 2; } // chroma row counted 2x per luma row
-    long long v = 0;
-    for(int k = 0; k < kStatsThreads / 32; k++) v += is_ssd ? (long long)s_ssd[k][src_r * 3 + c] : (long long)s_sd[k][src_r * 3 + c];
-    if(y + r < J.H) J.stat_rows[(int64_t)(y + r) * 6 + q] = v * mult;
-  }
-  // zero this row pair's CPS accumulators for the CPS kernel that follows
-  if((J.metrics & (QMIV_M_IVPSNR | QMIV_M_IVSSIM)) && threadIdx.x >= 32 && threadIdx.x < 44)
-  {
-    const int t = threadIdx.x - 32, dir = t / 6, r = (t % 6) / 3, c = t % 3;
-    if(y + r < J.H) J.cps_rows[((int64_t)dir * J.H + y + r) * 3 + c] = 0ull;
+    // zero this row pair's CPS accumulators for the CPS kernel that follows
+    if((J.metrics & (QMIV_M_IVPSNR | QMIV_M_IVSSIM)) && lane >= 16 && lane < 28)
+    {
+      const int t = lane - 16, dir = t / 6, r = (t % 6) / 3, c = t % 3;
+      if(y + r < J.H) J.cps_rows[((int64_t)dir * J.H + y + r) * 3 + c] = 0ull;
+    }
   }
 
   __threadfence();

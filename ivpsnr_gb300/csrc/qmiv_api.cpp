@@ -138,6 +138,7 @@ void derive_params(qmiv_handle* h)
   p.key_m_log2 = pow2_log2(p.key_m);
   p.luma_scale = (int32_t)(w0 * m);
   p.luma_scale_log2 = pow2_log2((uint64_t)p.luma_scale);
+  p.one = 1;
 }
 
 // Does the 32-bit packed key hold for this bit depth?
@@ -276,7 +277,7 @@ void plan_grid(qmiv_handle* h, DevJob* jobs, int n, const std::vector<int>& vari
   for(int i = 0; i < n; i++)
   {
     DevJob& j = jobs[i];
-    j.stat_blocks = (j.H + 1) / 2;
+    j.stat_blocks = ((j.H + 1) / 2 + 7) / 8; // 8 row pairs (one per warp) per block
     j.stat_base = sbase;
     sbase += j.stat_blocks;
     const int rows = variants()[variant[i]].rows;

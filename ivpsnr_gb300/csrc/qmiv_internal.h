@@ -56,6 +56,7 @@ struct Params {
   int32_t key_m_log2;                 // log2(M) if M is a power of two, else -1
   int32_t luma_scale;                 // s
   int32_t luma_scale_log2;            // log2(s) if s is a power of two, else -1
+  uint32_t one;                       // 1, opaque to the compiler (keeps index adds on the multiply-add pipe)
 };
 
 // Host-side launchers (defined in the .cu files).

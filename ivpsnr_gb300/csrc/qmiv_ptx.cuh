@@ -53,5 +53,13 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const void* tmap, int x, 
                :: "r"(smem_addr(dst)), "l"(tmap), "r"(x), "r"(y), "r"(smem_addr(bar)) : "memory");
 }
 
+// a*b+c as an integer multiply-add (issued to the FMA pipe rather than the ALU pipe)
+__device__ __forceinline__ unsigned mad_u32(unsigned a, unsigned b, unsigned c)
+{
+  unsigned d;
+  asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+  return d;
+}
+
 }  // namespace ptx
 }  // namespace qmiv
