@@ -39,6 +39,8 @@ struct TGeo {
   static constexpr int CTH  = fdiv2(R - 1 + SR) + CS + 1;      // chroma rows staged
   static constexpr int CRW  = 32 + 2 * XA;                     // raw chroma box width
   static constexpr int NC   = fdiv2(1 + SR) + CS + 1;          // chroma samples a quad's window spans per axis
+  static constexpr int KS_LOG2 = (2 * SR + 1) <= 4 ? 2 : ((2 * SR + 1) <= 8 ? 3 : 4);
+  static constexpr int KS   = 1 << KS_LOG2;                    // window-index row pitch (power of two)
   static constexpr int LBOX = (TH * RW * SB + 127) / 128 * 128;
   static constexpr int CBOX = (CTH * CRW * SB + 127) / 128 * 128;
   static constexpr int STAGE = 2 * LBOX + 4 * CBOX;
@@ -78,7 +80,6 @@ k_cps420_tma(const DevJob* __restrict__ jobs, int njobs, Params p)
   const int gs = dir == 0 ? 1 : -1;
   const int gd0 = gs * J.sc->gcd[0], gd1 = gs * J.sc->gcd[1], gd2 = gs * J.sc->gcd[2];
   const int s = p.luma_scale;
-  const unsigned one = p.one;
   const KeyT Mw1 = (KeyT)p.key_m * (KeyT)p.w_search[1];
   const KeyT Mw2 = (KeyT)p.key_m * (KeyT)p.w_search[2];
   const int mx = (1 << J.bd) - 1;
@@ -217,15 +218,17 @@ k_cps420_tma(const DevJob* __restrict__ jobs, int njobs, Params p)
               #pragma unroll
               for(int dx = -SR; dx <= SR; dx++)
               {
-                const int k = (dy + SR) * W2 + (dx + SR);
+                // window index with a power-of-two row pitch: same order as the row-major scan
+                const int k = (dy + SR) * G::KS + (dx + SR);
                 const int jc = fdiv2(px + dx) + G::CS;
                 const int dd = tY[a][px] - r[px + dx + SR];
-                KeyT key;
-                // the ALU pipe carries the difference and the min; the index add and the
-                // square go to the multiply-add pipe, so both pipes share the candidate loop
-                if(sizeof(KeyT) == 4) key = (KeyT)(unsigned)(dd * dd) + (KeyT)ptx::mad_u32((unsigned)B[jr][jc], one, (unsigned)k);
-                else                  key = (KeyT)((long long)dd * dd) + (B[jr][jc] + (KeyT)k);
-                best[a][px] = min(best[a][px], key);
+                // (dd^2 + chroma) is one multiply-add; "+ k, min" fuses into one add-min
+                if(sizeof(KeyT) == 4)
+                {
+                  const unsigned t = (unsigned)(dd * dd) + (unsigned)B[jr][jc];
+                  best[a][px] = min((unsigned)best[a][px], t + (unsigned)k);
+                }
+                else best[a][px] = min(best[a][px], (KeyT)((long long)dd * dd) + B[jr][jc] + (KeyT)k);
               }
           }
         }
@@ -238,9 +241,10 @@ k_cps420_tma(const DevJob* __restrict__ jobs, int njobs, Params p)
           for(int px = 0; px < 2; px++)
           {
             const int y = yq + a, x = cx0 + 2 * lane + px;
+            const bool valid = y < H && x < W;
             const unsigned k = p.key_m_log2 >= 0 ? (unsigned)(best[a][px] & (KeyT)(p.key_m - 1))
                                                  : (unsigned)(best[a][px] % (KeyT)p.key_m);
-            const int dy = (int)(k / W2) - SR, dx = (int)(k % W2) - SR;
+            const int dy = (int)(k >> G::KS_LOG2) - SR, dx = (int)(k & (G::KS - 1)) - SR;
             const int rl = cvtR[(2 * qr + a + SR + dy) * G::TW + 2 * lane + px + SR + dx];
             const int crow = clampi(qc + ((a + dy) >> 1), 0, Hc - 1) - cry0;
             const int ccl = clampi(cxh + lane + ((px + dx) >> 1), 0, Wc - 1) - crx0;
@@ -249,16 +253,14 @@ k_cps420_tma(const DevJob* __restrict__ jobs, int njobs, Params p)
             if(p.luma_scale_log2 >= 0) { rY = rl >> p.luma_scale_log2; tYr = tY[a][px] >> p.luma_scale_log2; }
             else                       { rY = rl / s; tYr = tY[a][px] / s; }
             const int d0 = tYr - rY, d1 = tCb - rcb, d2 = tCr - rcr;
-            if(y < H && x < W)
-            {
-              sq[a][0] += (unsigned)(d0 * d0); sq[a][1] += (unsigned)(d1 * d1); sq[a][2] += (unsigned)(d2 * d2);
-              if(want_scp)
-              { // clipU(ref - GCD) (xShftCompPic.cpp:88-92); for T2R the shift is -GCD
-                const int64_t o = (int64_t)y * J.scp_stride + x;
-                scp[0][o] = (uint16_t)clampi(rY - gd0, 0, mx);
-                scp[1][o] = (uint16_t)clampi(rcb - gd1, 0, mx);
-                scp[2][o] = (uint16_t)clampi(rcr - gd2, 0, mx);
-              }
+            const unsigned vm = valid ? 0xFFFFFFFFu : 0u;
+            sq[a][0] += (unsigned)(d0 * d0) & vm; sq[a][1] += (unsigned)(d1 * d1) & vm; sq[a][2] += (unsigned)(d2 * d2) & vm;
+            if(want_scp && valid)
+            { // clipU(ref - GCD) (xShftCompPic.cpp:88-92); for T2R the shift is -GCD
+              const int64_t o = (int64_t)y * J.scp_stride + x;
+              scp[0][o] = (uint16_t)clampi(rY - gd0, 0, mx);
+              scp[1][o] = (uint16_t)clampi(rcb - gd1, 0, mx);
+              scp[2][o] = (uint16_t)clampi(rcr - gd2, 0, mx);
             }
           }
         #pragma unroll

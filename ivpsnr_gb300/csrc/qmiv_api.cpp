@@ -112,6 +112,16 @@ struct qmiv_handle {
 namespace {
 
 int pow2_log2(uint64_t v) { if(v == 0 || (v & (v - 1))) return -1; int l = 0; while((1ull << l) < v) l++; return l; }
+
+// One past the largest window index: (2B+1)^2 for the row-major numbering, or 2B*P + 2B + 1
+// with the power-of-two row pitch P >= 2B+1 of the TMA kernels (the larger of the two).
+uint64_t window_index_bound(int sr)
+{
+  uint64_t pitch = 1;
+  while(pitch < (uint64_t)(2 * sr + 1)) pitch <<= 1;
+  const uint64_t a = (uint64_t)(2 * sr + 1) * (2 * sr + 1), b = 2ull * sr * pitch + 2ull * sr + 1;
+  return a > b ? a : b;
+}
 int32_t rne_f32(float v) { return (int32_t)std::nearbyint(v); }
 
 void derive_params(qmiv_handle* h)
@@ -129,8 +139,9 @@ void derive_params(qmiv_handle* h)
     }
   p.fake_exact = o.fake_exact;
   p.legacy_ws8 = o.legacy_ws8;
-  // CPS key: M*E + k with k < N = (2B+1)^2 and (s*d)^2 = M*w0*d^2, s = w0*m, M = w0*m^2
-  const uint64_t N = (uint64_t)(2 * o.search_range + 1) * (2 * o.search_range + 1);
+  // CPS key: M*E + k with (s*d)^2 = M*w0*d^2, s = w0*m, M = w0*m^2, and M above every window
+  // index k; the TMA kernels number the window with a power-of-two row pitch, so k < N
+  const uint64_t N = window_index_bound(o.search_range);
   const uint64_t w0 = (uint64_t)std::max(o.cmp_w_search[0], 1);
   uint64_t m = 1;
   while(w0 * m * m < N) m <<= 1;
@@ -149,7 +160,7 @@ bool key32_ok(const qmiv_handle* h, int bd)
   for(int c = 0; c < 3; c++) md = std::max(md, p.maxdiff_for_bd[bd][c]);
   const uint64_t D = (uint64_t)((1 << bd) - 1) + (uint64_t)md;
   const uint64_t wsum = (uint64_t)p.w_search[0] + p.w_search[1] + p.w_search[2];
-  const uint64_t N = (uint64_t)(2 * p.sr + 1) * (2 * p.sr + 1);
+  const uint64_t N = window_index_bound(p.sr);
   const uint64_t kmax = (uint64_t)p.key_m * wsum * D * D + N;
   return kmax < (1ull << 32) && (uint64_t)p.luma_scale * D < 46340ull;
 }
