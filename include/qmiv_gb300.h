@@ -77,6 +77,9 @@ typedef struct qmiv_options {
   int32_t fake_exact;      /* 1 (default): exact components report PSNR(SSD=1) as the application does */
   int32_t legacy_ws8;      /* setLegacyWS8bit (off by default, never set by the application) */
   int32_t ssim_window;     /* QMIV_SSIM_REF10 (default) or QMIV_SSIM_GAUSS11 */
+  uint32_t scratch_metrics;/* metrics whose per-job device scratch qmiv_create reserves (default
+                            * QMIV_M_ALL); the SSIM family needs shift-compensated pictures and the
+                            * MS-SSIM pyramid for every job slot, so PSNR-only callers can skip it */
 } qmiv_options;
 
 /* Per-frame results. Per-component arrays hold Y, Cb, Cr (index 3 unused, 0). The *_pic

@@ -27,7 +27,7 @@ class Pic(ctypes.Structure):
 class Options(ctypes.Structure):
     _fields_ = [("search_range", c_i32), ("cmp_w_search", c_i32 * 4), ("cmp_w_avg", c_i32 * 4),
                 ("unnoticeable", c_f32 * 4), ("use_ws", c_i32), ("lon_deg", c_i32), ("lat_deg", c_i32),
-                ("fake_exact", c_i32), ("legacy_ws8", c_i32), ("ssim_window", c_i32)]
+                ("fake_exact", c_i32), ("legacy_ws8", c_i32), ("ssim_window", c_i32), ("scratch_metrics", c_u32)]
 
 
 class FrameResult(ctypes.Structure):

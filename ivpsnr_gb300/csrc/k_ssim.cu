@@ -1,0 +1,280 @@
+// SSIM family kernels: windowed structural similarity (libs/pmbb-ivqm/src/xStructSim.cpp:15-60),
+// its picture mean (xSSIM.cpp:91-140), the MS-SSIM pyramid (xSSIM.cpp:67-87,142-148 with
+// DownsampleHV, libs/pmbb-core/src/xPixelOpsSTD.cpp:50-67) and the IV-SSIM combination
+// (xSSIM.cpp:166-210).
+//
+// The reference evaluates 10x10 (REF10) window moments in FP64 with FP32 coefficients per
+// output pixel (800 multiply-adds). Here the window is separable: the coefficient table is
+// the outer product of the normalised 11-tap Gaussian g rounded to 10 decimals, so the
+// moments are computed as a horizontal then a vertical 10-tap (or 11-tap) pass in FP32
+// (~100 multiply-adds per pixel), on samples centred by a per-tile integer offset c so that
+// E[x^2] - E[x]^2 does not cancel. With W0 = (sum g)^2 the moments about zero follow from
+// the centred sums S1 = sum w (x-c), S2 = sum w (x-c)^2:
+//   mu  = S1 + c W0,   var = S2 - S1^2 + (1-W0)(2c S1 + c^2 W0),
+//   cov = Sxy - S1x S1y + (1-W0)(c (S1x + S1y) + c^2 W0).
+// Rows are summed per 32-pixel tile in FP32 and across tiles and rows in FP64 (compensated),
+// the picture sum divided by W*H as the reference does.
+#include <cfloat>
+
+#include "qmiv_device.cuh"
+#include "qmiv_ssim.h"
+
+namespace qmiv {
+
+__constant__ float c_g[11];      // 1-D window factor
+__constant__ float c_w0[2];      // W0 = (sum g)^2 for the 10- and 11-tap windows
+__constant__ float c_om[2];      // 1 - W0, rounded from FP64 (not formed in FP32)
+__constant__ double c_w0d[2];
+__constant__ double c_omd[2];
+
+namespace {
+
+constexpr int kTX = 32, kTY = 32, kThreads = 256;
+
+__device__ __forceinline__ int ld_plane(const SsimPlane& p, int x, int y)
+{
+  const int64_t o = (int64_t)(y >> p.shift) * p.stride + (x >> p.shift);
+  return p.sbytes == 1 ? (int)__ldg((const uint8_t*)p.ptr + o) : (int)__ldg((const uint16_t*)p.ptr + o);
+}
+
+__device__ __forceinline__ int find_ssim_job(const SsimJob* __restrict__ jobs, int n, int b)
+{
+  int lo = 0, hi = n - 1;
+  while(lo < hi) { const int mid = (lo + hi + 1) >> 1; if(jobs[mid].tile_base <= b) lo = mid; else hi = mid - 1; }
+  return lo;
+}
+
+template <int WIN>
+__global__ void __launch_bounds__(kThreads) k_ssim(const SsimJob* __restrict__ jobs, int njobs)
+{
+  constexpr int IW = kTX + WIN - 1, IH = kTY + WIN - 1;   // staged input tile
+  __shared__ float s_in[2][IH][IW + 1];
+  __shared__ float s_h[5][IH][kTX + 1];
+  __shared__ int s_c;
+
+  const int jb = find_ssim_job(jobs, njobs, blockIdx.x);
+  const SsimJob& J = jobs[jb];
+  const int local = blockIdx.x - J.tile_base;
+  const int ty = local / J.tiles_x, tx = local - ty * J.tiles_x;
+  const int W = J.W, H = J.H;
+  const int x0 = 5 + tx * kTX, y0 = 5 + ty * kTY;
+  const int x1 = min(x0 + kTX, W - 5), y1 = min(y0 + kTY, H - 5);
+  const int tid = threadIdx.x;
+
+  if(tid == 0) s_c = ld_plane(J.b, min((x0 + x1) >> 1, W - 1), min((y0 + y1) >> 1, H - 1));
+  __syncthreads();
+  const int c = s_c;
+  for(int i = tid; i < IH * IW; i += kThreads)
+  {
+    const int r = i / IW, q = i - r * IW;
+    const int gx = min(x0 - 5 + q, W - 1), gy = min(y0 - 5 + r, H - 1);
+    s_in[0][r][q] = (float)(ld_plane(J.a, gx, gy) - c);
+    s_in[1][r][q] = (float)(ld_plane(J.b, gx, gy) - c);
+  }
+  __syncthreads();
+
+  // horizontal pass: 4 consecutive output columns of one input row per work item
+  for(int item = tid; item < IH * (kTX / 4); item += kThreads)
+  {
+    const int r = item / (kTX / 4), q0 = (item - r * (kTX / 4)) * 4;
+    float a[4 + WIN - 1], b[4 + WIN - 1];
+    #pragma unroll
+    for(int i = 0; i < 4 + WIN - 1; i++) { a[i] = s_in[0][r][q0 + i]; b[i] = s_in[1][r][q0 + i]; }
+    #pragma unroll
+    for(int o = 0; o < 4; o++)
+    {
+      float m0 = 0.f, m1 = 0.f, m2 = 0.f, m3 = 0.f, m4 = 0.f;
+      #pragma unroll
+      for(int k = 0; k < WIN; k++)
+      {
+        const float g = c_g[k], av = a[o + k], bv = b[o + k];
+        const float ga = g * av, gb = g * bv;
+        m0 += ga; m1 += gb;
+        m2 = fmaf(ga, av, m2); m3 = fmaf(gb, bv, m3); m4 = fmaf(ga, bv, m4);
+      }
+      s_h[0][r][q0 + o] = m0; s_h[1][r][q0 + o] = m1; s_h[2][r][q0 + o] = m2;
+      s_h[3][r][q0 + o] = m3; s_h[4][r][q0 + o] = m4;
+    }
+  }
+  __syncthreads();
+
+  // vertical pass: one column, 4 output rows per thread
+  const int col = tid & 31, rg = tid >> 5;                 // 8 row groups of 4 rows
+  float acc[4][5];
+  #pragma unroll
+  for(int o = 0; o < 4; o++)
+    #pragma unroll
+    for(int m = 0; m < 5; m++) acc[o][m] = 0.f;
+  #pragma unroll
+  for(int i = 0; i < 4 + WIN - 1; i++)
+  {
+    const int r = rg * 4 + i;
+    float hv[5];
+    #pragma unroll
+    for(int m = 0; m < 5; m++) hv[m] = s_h[m][r][col];
+    #pragma unroll
+    for(int o = 0; o < 4; o++)
+    {
+      const int k = i - o;
+      if(k < 0 || k >= WIN) continue;
+      const float g = c_g[k];
+      #pragma unroll
+      for(int m = 0; m < 5; m++) acc[o][m] = fmaf(g, hv[m], acc[o][m]);
+    }
+  }
+
+  const int wi = WIN == 11 ? 1 : 0;
+  const float w0 = c_w0[wi];
+  const float om = c_om[wi];
+  const float cf = (float)c;
+  const float k_cc = (float)(c_omd[wi] * (double)c * (double)c * c_w0d[wi]);
+  const float cw0 = cf * w0;
+  const float C1 = J.c1, C2 = J.c2;
+  float rows[4];
+  #pragma unroll
+  for(int o = 0; o < 4; o++)
+  {
+    const float S1a = acc[o][0], S1b = acc[o][1], S2a = acc[o][2], S2b = acc[o][3], Sab = acc[o][4];
+    const float mua = S1a + cw0, mub = S1b + cw0;
+    const float va = S2a - S1a * S1a + fmaf(om * 2.0f * cf, S1a, k_cc);
+    const float vb = S2b - S1b * S1b + fmaf(om * 2.0f * cf, S1b, k_cc);
+    const float cov = Sab - S1a * S1b + fmaf(om * cf, S1a + S1b, k_cc);
+    float v = __fdiv_rn(2.0f * cov + C2, va + vb + C2);
+    if(J.calc_l) v *= __fdiv_rn(2.0f * mua * mub + C1, mua * mua + mub * mub + C1);
+    const int y = y0 + rg * 4 + o, x = x0 + col;
+    rows[o] = (y < y1 && x < x1) ? v : 0.0f;
+  }
+  #pragma unroll
+  for(int o = 0; o < 4; o++)
+  {
+    float s = rows[o];
+    #pragma unroll
+    for(int d = 16; d > 0; d >>= 1) s += __shfl_xor_sync(0xffffffffu, s, d);
+    const int y = y0 + rg * 4 + o;
+    if(col == 0 && y < y1) J.partial[(int64_t)(y - 5) * J.tiles_x + tx] = s;
+  }
+}
+
+// Picture sum of one SSIM job: rows summed over their tiles in FP64 (fixed order), rows combined
+// with a compensated sum, divided by W*H (xSSIM.cpp:106-111).
+__global__ void __launch_bounds__(256) k_ssim_finalize(const SsimJob* __restrict__ jobs, int njobs)
+{
+  __shared__ double scratch[16];
+  const SsimJob& J = jobs[blockIdx.x];
+  const int rows = max(0, J.H - 10);
+  Kbns k = { 0.0, 0.0 };
+  for(int r = threadIdx.x; r < rows; r += blockDim.x)
+  {
+    double s = 0.0;
+    for(int t = 0; t < J.tiles_x; t++) s = __dadd_rn(s, (double)__ldcg(J.partial + (int64_t)r * J.tiles_x + t));
+    k = kbns_add(k, s);
+  }
+  const double tot = block_kbns(k, scratch);
+  if(threadIdx.x == 0) *J.out = __ddiv_rn(tot, (double)((int64_t)J.W * J.H));
+}
+
+// DownsampleHV to a 16-bit plane: d(x,y) = (s(2x,2y)+s(2x+1,2y)+s(2x,2y+1)+s(2x+1,2y+1)+2)>>2
+__global__ void __launch_bounds__(256) k_downsample(const PyrStep* __restrict__ steps, int nsteps)
+{
+  const PyrStep& S = steps[blockIdx.y];
+  const int x = blockIdx.x * 64 + (threadIdx.x & 63);
+  for(int y = threadIdx.x >> 6; y < S.dh; y += 4)
+  {
+    if(x >= S.dw) break;
+    const int sx = 2 * x, sy = 2 * y;
+    const int v = ld_plane(S.src, sx, sy) + ld_plane(S.src, sx + 1, sy) + ld_plane(S.src, sx, sy + 1) + ld_plane(S.src, sx + 1, sy + 1);
+    S.dst[(int64_t)y * S.dst_stride + x] = (uint16_t)((v + 2) >> 2);
+  }
+}
+
+// Per frame: SSIM, MS-SSIM (product of per-scale scores to the scale weights,
+// xStructSimConsts.h:27) and IV-SSIM (weighted, worse of both directions).
+__global__ void k_ssim_combine(const SsimFrame* __restrict__ frames, int nframes, Params p)
+{
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if(f >= nframes) return;
+  const SsimFrame& F = frames[f];
+  qmiv_frame_result* R = F.result;
+  const double* v = F.vals;
+  if(F.metrics & QMIV_M_SSIM)
+  {
+    double s[3] = { v[0], v[1], v[2] };
+    for(int c = 0; c < 3; c++) R->ssim[c] = s[c];
+    R->ssim[3] = 0.0;
+    R->ssim_pic = weighted3(s, p.w_avg);
+  }
+  if(F.metrics & QMIV_M_MSSSIM)
+  {
+    const double wts[5] = { 0.0448, 0.2856, 0.3001, 0.2363, 0.1333 };
+    double m[3];
+    for(int c = 0; c < 3; c++)
+    {
+      double acc = 1.0;
+      for(int i = 0; i < 5; i++) acc = __dmul_rn(acc, pow(v[3 + i * 3 + c], wts[i]));
+      m[c] = acc;
+      R->msssim[c] = acc;
+    }
+    R->msssim[3] = 0.0;
+    R->msssim_pic = weighted3(m, p.w_avg);
+  }
+  if(F.metrics & QMIV_M_IVSSIM)
+  {
+    const double t2r[3] = { v[18], v[19], v[20] }, r2t[3] = { v[21], v[22], v[23] };
+    const double a = weighted3(t2r, p.w_avg), b = weighted3(r2t, p.w_avg);
+    R->ivssim_t2r = a;
+    R->ivssim_r2t = b;
+    R->ivssim = b < a ? b : a; // std::min(SSIM_T2R, SSIM_R2T) (xSSIM.cpp:205)
+  }
+}
+
+}  // namespace
+
+cudaError_t ssim_set_window_constants(const float g[11], const double w0[2])
+{
+  const float w0f[2] = { (float)w0[0], (float)w0[1] };
+  const double omd[2] = { 1.0 - w0[0], 1.0 - w0[1] };
+  const float omf[2] = { (float)omd[0], (float)omd[1] };
+  cudaError_t e = cudaMemcpyToSymbol(c_g, g, sizeof(float) * 11);
+  if(e == cudaSuccess) e = cudaMemcpyToSymbol(c_w0, w0f, sizeof(w0f));
+  if(e == cudaSuccess) e = cudaMemcpyToSymbol(c_om, omf, sizeof(omf));
+  if(e == cudaSuccess) e = cudaMemcpyToSymbol(c_w0d, w0, sizeof(double) * 2);
+  if(e == cudaSuccess) e = cudaMemcpyToSymbol(c_omd, omd, sizeof(omd));
+  return e;
+}
+
+int ssim_tiles_x(int W) { return W > 10 ? (W - 10 + kTX - 1) / kTX : 0; }
+int ssim_tiles_y(int H) { return H > 10 ? (H - 10 + kTY - 1) / kTY : 0; }
+
+cudaError_t launch_ssim(const SsimJob* d_jobs, const SsimJob* h_jobs, int n, int window, cudaStream_t st)
+{
+  int blocks = 0;
+  for(int i = 0; i < n; i++) blocks = h_jobs[i].tile_base + h_jobs[i].tiles_x * h_jobs[i].tiles_y;
+  if(blocks > 0)
+  {
+    if(window == QMIV_SSIM_GAUSS11) k_ssim<11><<<blocks, kThreads, 0, st>>>(d_jobs, n);
+    else                            k_ssim<10><<<blocks, kThreads, 0, st>>>(d_jobs, n);
+    cudaError_t e = cudaGetLastError();
+    if(e != cudaSuccess) return e;
+  }
+  k_ssim_finalize<<<n, 256, 0, st>>>(d_jobs, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_downsample(const PyrStep* d_steps, const PyrStep* h_steps, int n, cudaStream_t st)
+{
+  int maxw = 0;
+  for(int i = 0; i < n; i++) maxw = h_steps[i].dw > maxw ? h_steps[i].dw : maxw;
+  if(n == 0 || maxw == 0) return cudaSuccess;
+  dim3 grid((maxw + 63) / 64, n);
+  k_downsample<<<grid, 256, 0, st>>>(d_steps, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ssim_combine(const SsimFrame* d_frames, int n, const Params& p, cudaStream_t st)
+{
+  if(n == 0) return cudaSuccess;
+  k_ssim_combine<<<(n + 63) / 64, 64, 0, st>>>(d_frames, n, p);
+  return cudaGetLastError();
+}
+
+}  // namespace qmiv

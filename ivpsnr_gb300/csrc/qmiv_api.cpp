@@ -1,6 +1,7 @@
 // Host side of the C ABI (include/qmiv_gb300.h): handles, argument validation, device
 // scratch, job descriptors and launch sequencing. No host threads; every call is enqueued
-// on the caller's stream.
+// on the caller's stream. Calls on one handle must be issued on one stream (or serialised):
+// they share the handle's device job tables.
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
@@ -14,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include "qmiv_internal.h"
+#include "qmiv_ssim.h"
 
 using namespace qmiv;
 
@@ -67,17 +69,33 @@ qmiv_status fail(qmiv_status s, const char* fmt, ...)
     if(e_ != cudaSuccess) return fail(QMIV_CUDA_ERROR, "%s: %s", #expr, cudaGetErrorString(e_)); \
   } while(0)
 
-// Device slot for one job: scratch rows and scalars, plus the tensor maps of its planes.
+size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+constexpr uint32_t kSsimMetrics = QMIV_M_SSIM | QMIV_M_MSSSIM | QMIV_M_IVSSIM;
+constexpr int kSsimJobsPerFrame = 24;  // 3 SSIM + 15 MS-SSIM + 6 IV-SSIM
+constexpr int kPyrStepsPerFrame = 6;   // per pyramid level: 2 pictures x 3 components
+
+// Device slot for one job: scratch rows and scalars, tensor maps, SSIM scratch.
 struct Slot {
-  int64_t* stat_rows = nullptr;          // [max_h][6]
+  int64_t* stat_rows = nullptr;           // [max_h][6]
   unsigned long long* cps_rows = nullptr; // [2][max_h][3]
   JobScalars* sc = nullptr;
-  void* d_tmaps = nullptr;               // 6 x 128 B in device memory
-  uint64_t tmap_key[16] = { 0 };         // what the maps were encoded for
+  void* d_tmaps = nullptr;                // 6 x 128 B
+  uint64_t tmap_key[16] = { 0 };
   bool tmap_valid = false;
+  uint16_t* scp = nullptr;                // 2 pictures x 3 planes x max_w*max_h (IV-SSIM)
+  uint16_t* pyr = nullptr;                // MS-SSIM levels 1..4, 2 pictures x 3 components
+  float* partial = nullptr;               // SSIM per-tile row sums of all the frame's SSIM jobs
+  double* vals = nullptr;                 // kSsimVals picture means
 };
 
-struct SeqAcc { std::vector<double> v[16]; };
+struct SeqAcc { std::vector<double> v[18]; };
+
+// Per-call tables uploaded to the device in one copy, from a ring of pinned buffers so that
+// a table is never rewritten while an earlier call's copy of it may still be pending.
+struct CallTables {
+  size_t jobs_off, ssim_off, pyr_off, frames_off, bytes;
+};
 
 }  // namespace
 
@@ -86,23 +104,31 @@ struct qmiv_handle {
   Params params;
   int max_w = 0, max_h = 0, max_jobs = 0;
   int device = 0, num_sms = 0;
-  int cps_variant_override = -1;         // set by the autotuner / tests
+  int cps_variant_override = -1;
   std::vector<Slot> slots;
   void* slot_mem = nullptr;
-  DevJob* d_jobs = nullptr;              // device job table
-  DevJob* h_jobs = nullptr;              // pinned host job table
+  void* ssim_mem = nullptr;
+  size_t slot_partial_floats = 0;
   qmiv_frame_result* d_results = nullptr;
   qmiv_frame_result* h_results = nullptr; // pinned
-  // staging for host pictures (2 pictures, planar, uint16 worst case)
+  // call tables
+  CallTables tab;
+  uint8_t* d_tab = nullptr;
+  static constexpr int kRing = 4;
+  uint8_t* h_tab[kRing] = { nullptr };
+  cudaEvent_t tab_ev[kRing] = { nullptr };
+  bool tab_used[kRing] = { false };
+  int tab_next = 0;
+  // host-side working copies of the tables
+  std::vector<DevJob> jobs;
+  std::vector<SsimJob> sjobs;
+  std::vector<PyrStep> steps[4];
+  std::vector<SsimFrame> frames;
+  // staging for host pictures (2 pictures, planar, up to uint16 4:4:4)
   uint16_t* d_stage[2] = { nullptr, nullptr };
-  size_t stage_elems = 0;
-  // shift-compensated pictures for the per-frame IV-SSIM path
-  uint16_t* d_scp[2] = { nullptr, nullptr };
-  // equirectangular row weights, cached per (height, lat)
   std::map<std::pair<int, int>, std::pair<double*, double>> ws_cache;
   SeqAcc seq;
   int64_t launches = 0;
-  // optional per-launch timing
   struct Prof { cudaEvent_t a = nullptr, b = nullptr; const char* name = ""; };
   bool profiling = false;
   std::vector<Prof> prof;
@@ -234,6 +260,17 @@ qmiv_status check_pair(const qmiv_handle* h, const qmiv_pic* a, const qmiv_pic* 
   return QMIV_OK;
 }
 
+qmiv_status check_metrics(const qmiv_handle* h, uint32_t metrics, int W, int H)
+{
+  if(metrics & ~QMIV_M_ALL) return fail(QMIV_BAD_ARG, "metrics 0x%x", metrics);
+  if(metrics & ~h->opt.scratch_metrics)
+    return fail(QMIV_UNSUPPORTED, "metrics 0x%x need scratch the handle did not reserve (scratch_metrics 0x%x)",
+                metrics, h->opt.scratch_metrics);
+  if((metrics & QMIV_M_MSSSIM) && (W < 16 || H < 16))
+    return fail(QMIV_UNSUPPORTED, "MS-SSIM needs at least 16x16 (four halvings), got %dx%d", W, H);
+  return QMIV_OK;
+}
+
 qmiv_status ws_weights(qmiv_handle* h, int H, const double** d_w, double* corr)
 {
   const auto key = std::make_pair(H, h->opt.lat_deg);
@@ -262,7 +299,7 @@ qmiv_status ws_weights(qmiv_handle* h, int H, const double** d_w, double* corr)
   return QMIV_OK;
 }
 
-// Fill the device-independent part of a job from two validated pictures (device pointers).
+// Fill a job from two validated device pictures.
 void fill_job(qmiv_handle* h, DevJob& j, const qmiv_pic* a, const qmiv_pic* b, uint32_t metrics, int slot)
 {
   std::memset(&j, 0, sizeof(j));
@@ -274,6 +311,7 @@ void fill_job(qmiv_handle* h, DevJob& j, const qmiv_pic* a, const qmiv_pic* b, u
   j.W = a->width; j.H = a->height; j.bd = a->bitdepth; j.sbytes = a->sample_bytes;
   j.cshift = a->chroma_format == QMIV_CF420 ? 1 : 0;
   j.metrics = metrics;
+  j.slot = slot;
   j.stat_rows = h->slots[slot].stat_rows;
   j.cps_rows = h->slots[slot].cps_rows;
   j.sc = h->slots[slot].sc;
@@ -306,7 +344,7 @@ void plan_grid(qmiv_handle* h, DevJob* jobs, int n, const std::vector<int>& vari
       continue;
     }
     const int nchunks = (j.W + 63) / 64;
-    int segs = (int)std::min<long long>(nchunks, std::max<long long>(1, (target + strips_total - 1) / strips_total));
+    int segs = (int)std::min<long long>(nchunks, std::max<long long>(1, (target + strips_total - 1) / std::max(1ll, strips_total)));
     // per-thread 32-bit SSE accumulators: 2 pixels per chunk, each < (Max + maxdiff)^2
     int md = 0; for(int c = 0; c < 3; c++) md = std::max(md, h->params.maxdiff_for_bd[j.bd][c]);
     const double D = (double)((1 << j.bd) - 1 + md);
@@ -319,7 +357,7 @@ void plan_grid(qmiv_handle* h, DevJob* jobs, int n, const std::vector<int>& vari
 }
 
 qmiv_status upload_pic(qmiv_handle* h, const qmiv_pic* src, int idx, qmiv_pic* dst, cudaStream_t st)
-{ // host picture -> packed device staging (same sample size, planes back to back)
+{ // host picture -> packed device staging (same sample size, planes back to back, 16-byte rows aligned)
   *dst = *src;
   if(src->is_device) return QMIV_OK;
   const int sb = src->sample_bytes;
@@ -329,18 +367,18 @@ qmiv_status upload_pic(qmiv_handle* h, const qmiv_pic* src, int idx, qmiv_pic* d
   {
     const int w = (c && src->chroma_format == QMIV_CF420) ? src->width / 2 : src->width;
     const int hh = (c && src->chroma_format == QMIV_CF420) ? src->height / 2 : src->height;
+    const int pitch = ((w * sb + 15) & ~15) / sb;  // rows of 16-byte multiples: TMA-eligible
     off = (off + 15) & ~(size_t)15;
-    CUDA_TRY(cudaMemcpy2DAsync(base + off, (size_t)w * sb, src->plane[c], (size_t)src->stride[c] * sb,
+    CUDA_TRY(cudaMemcpy2DAsync(base + off, (size_t)pitch * sb, src->plane[c], (size_t)src->stride[c] * sb,
                                (size_t)w * sb, hh, cudaMemcpyHostToDevice, st));
     dst->plane[c] = base + off;
-    dst->stride[c] = w;
-    off += (size_t)w * hh * sb;
+    dst->stride[c] = pitch;
+    off += (size_t)pitch * hh * sb;
   }
   dst->is_device = 1;
   return QMIV_OK;
 }
 
-// Event pair around one launch when profiling is enabled.
 cudaError_t prof_mark(qmiv_handle* h, const char* name, cudaStream_t st, bool begin)
 {
   if(!h->profiling) return cudaSuccess;
@@ -360,11 +398,11 @@ cudaError_t prof_mark(qmiv_handle* h, const char* name, cudaStream_t st, bool be
 }
 
 // Encode (or reuse) the six tensor maps a TMA variant reads for one job's planes.
-qmiv_status ensure_tmaps(qmiv_handle* h, int slot, DevJob& j, const CpsVariant& v, cudaStream_t st)
+qmiv_status ensure_tmaps(qmiv_handle* h, DevJob& j, const CpsVariant& v, cudaStream_t st)
 {
-  Slot& S = h->slots[slot];
+  Slot& S = h->slots[j.slot];
   const int sb = j.sbytes, XA = 16 / sb, R = v.rows, SR = v.sr, CS = (SR + 1) / 2;
-  const int fd = (R - 1 + SR) >= 0 ? (R - 1 + SR) / 2 : -((-(R - 1 + SR) + 1) / 2);
+  const int fd = (R - 1 + SR) / 2;
   const uint32_t RW = 64 + 2 * XA, TH = R + 2 * SR, CRW = 32 + 2 * XA, CTH = fd + CS + 1;
   uint64_t key[16] = { 0 };
   for(int c = 0; c < 3; c++)
@@ -401,62 +439,238 @@ qmiv_status ensure_tmaps(qmiv_handle* h, int slot, DevJob& j, const CpsVariant& 
   return QMIV_OK;
 }
 
-// Run stats + CPS for n jobs already in h->h_jobs[0..n) (slots 0..n).
-qmiv_status run_psnr_family(qmiv_handle* h, int n, cudaStream_t st)
+// ------------------------------------------------------------------------------------
+// SSIM-family planning
+// ------------------------------------------------------------------------------------
+SsimPlane plane_of(const void* p, int stride, int sbytes, int shift)
 {
+  SsimPlane s;
+  s.ptr = p; s.stride = stride; s.sbytes = (int8_t)sbytes; s.shift = (int8_t)shift; s.pad = 0;
+  return s;
+}
+
+void add_ssim_job(qmiv_handle* h, const SsimPlane& a, const SsimPlane& b, int W, int H, int bd, int calc_l,
+                  float*& partial, double* out)
+{
+  SsimJob s;
+  std::memset(&s, 0, sizeof(s));
+  s.a = a; s.b = b; s.W = W; s.H = H; s.calc_l = calc_l;
+  const double mx = (double)((1 << bd) - 1);
+  s.c1 = (float)((0.01 * mx) * (0.01 * mx)); // xSSIM.cpp:21-23
+  s.c2 = (float)((0.03 * mx) * (0.03 * mx));
+  s.tiles_x = ssim_tiles_x(W);
+  s.tiles_y = ssim_tiles_y(H);
+  s.partial = partial;
+  s.out = out;
+  partial += (size_t)std::max(0, H - 10) * s.tiles_x;
+  h->sjobs.push_back(s);
+}
+
+// SSIM jobs, pyramid steps and the combine entry of one frame (a job with SSIM metrics).
+qmiv_status plan_ssim(qmiv_handle* h, const DevJob& j)
+{
+  Slot& S = h->slots[j.slot];
+  const int W = j.W, H = j.H, bd = j.bd, sb = j.sbytes, cs = j.cshift;
+  float* part = S.partial;
+  const SsimPlane P0[3] = { plane_of(j.p0[0], j.stride0[0], sb, 0), plane_of(j.p0[1], j.stride0[1], sb, cs), plane_of(j.p0[2], j.stride0[2], sb, cs) };
+  const SsimPlane P1[3] = { plane_of(j.p1[0], j.stride1[0], sb, 0), plane_of(j.p1[1], j.stride1[1], sb, cs), plane_of(j.p1[2], j.stride1[2], sb, cs) };
+  if(j.metrics & QMIV_M_SSIM)   // xAppQMIV.cpp:907: calcPicSSIM(P0, P1)
+    for(int c = 0; c < 3; c++) add_ssim_job(h, P0[c], P1[c], W, H, bd, 1, part, S.vals + c);
+  if(j.metrics & QMIV_M_IVSSIM) // xSSIM.cpp:197-198: T2R = SSIM(P0, SCP1), R2T = SSIM(P1, SCP0)
+  {
+    for(int c = 0; c < 3; c++)
+    {
+      add_ssim_job(h, P0[c], plane_of(j.scp1[c], j.scp_stride, 2, 0), W, H, bd, 1, part, S.vals + 18 + c);
+      add_ssim_job(h, P1[c], plane_of(j.scp0[c], j.scp_stride, 2, 0), W, H, bd, 1, part, S.vals + 21 + c);
+    }
+  }
+  if(j.metrics & QMIV_M_MSSSIM) // xSSIM.cpp:67-87
+  {
+    for(int c = 0; c < 3; c++) add_ssim_job(h, P0[c], P1[c], W, H, bd, 0, part, S.vals + 3 + c);
+    // pyramid: level s of picture p, component c lives at pyr + off(s) + (p*3+c)*cap(s)
+    size_t off = 0;
+    SsimPlane prev[2][3];
+    for(int p = 0; p < 2; p++)
+      for(int c = 0; c < 3; c++) prev[p][c] = p == 0 ? plane_of(j.p0[c], j.stride0[c], sb, 0) : plane_of(j.p1[c], j.stride1[c], sb, 0);
+    int w = W, hh = H;
+    for(int s = 1; s <= 4; s++)
+    {
+      const int dw = w >> 1, dh = hh >> 1;
+      const size_t cap = (size_t)(h->max_w >> s) * (h->max_h >> s);
+      SsimPlane cur[2][3];
+      for(int p = 0; p < 2; p++)
+        for(int c = 0; c < 3; c++)
+        {
+          if(s == 1 && c > 0 && cs)
+          { // 4:2:0: the 2x2 mean of the nearest-neighbour upsampled chroma is the native plane
+            cur[p][c] = p == 0 ? plane_of(j.p0[c], j.stride0[c], sb, 0) : plane_of(j.p1[c], j.stride1[c], sb, 0);
+            continue;
+          }
+          uint16_t* dst = S.pyr + off + (size_t)(p * 3 + c) * cap;
+          PyrStep st;
+          st.src = prev[p][c]; st.dst = dst; st.dst_stride = dw; st.dw = dw; st.dh = dh;
+          h->steps[s - 1].push_back(st);
+          cur[p][c] = plane_of(dst, dw, 2, 0);
+        }
+      off += 6 * cap;
+      for(int c = 0; c < 3; c++) add_ssim_job(h, cur[0][c], cur[1][c], dw, dh, bd, s != 4, part, S.vals + 3 + 3 * s + c);
+      for(int p = 0; p < 2; p++) for(int c = 0; c < 3; c++) prev[p][c] = cur[p][c];
+      w = dw; hh = dh;
+    }
+  }
+  SsimFrame f;
+  f.metrics = j.metrics & kSsimMetrics; f.pad = 0; f.result = j.result; f.vals = S.vals;
+  h->frames.push_back(f);
+  return QMIV_OK;
+}
+
+// Lays out the call tables of h->jobs / sjobs / steps / frames and copies them to the device.
+qmiv_status upload_tables(qmiv_handle* h, cudaStream_t st)
+{
+  CallTables& t = h->tab;
+  const int k = h->tab_next;
+  h->tab_next = (k + 1) % qmiv_handle::kRing;
+  if(h->tab_used[k]) CUDA_TRY(cudaEventSynchronize(h->tab_ev[k]));
+  uint8_t* hb = h->h_tab[k];
+  size_t pos = 0;
+  auto put = [&](const void* src, size_t bytes) { std::memcpy(hb + pos, src, bytes); pos += align256(bytes); };
+  put(h->jobs.data(), sizeof(DevJob) * h->jobs.size());
+  put(h->sjobs.data(), sizeof(SsimJob) * h->sjobs.size());
+  for(int s = 0; s < 4; s++) put(h->steps[s].data(), sizeof(PyrStep) * h->steps[s].size());
+  put(h->frames.data(), sizeof(SsimFrame) * h->frames.size());
+  if(pos > t.bytes) return fail(QMIV_TOO_LARGE, "call tables %zu B > %zu B", pos, t.bytes);
+  CUDA_TRY(cudaMemcpyAsync(h->d_tab, hb, pos, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaEventRecord(h->tab_ev[k], st));
+  h->tab_used[k] = true;
+  return QMIV_OK;
+}
+
+// Runs every metric of the jobs in h->jobs (each bound to its slot).
+qmiv_status run_jobs(qmiv_handle* h, cudaStream_t st)
+{
+  const int n = (int)h->jobs.size();
   std::vector<int> var(n);
-  for(int i = 0; i < n; i++) var[i] = (h->h_jobs[i].metrics & (QMIV_M_IVPSNR | QMIV_M_IVSSIM)) ? pick_cps_variant(h, h->h_jobs[i]) : -1;
+  bool any_stats = false;
+  for(int i = 0; i < n; i++)
+  {
+    DevJob& j = h->jobs[i];
+    var[i] = (j.metrics & (QMIV_M_IVPSNR | QMIV_M_IVSSIM)) ? pick_cps_variant(h, j) : -1;
+    any_stats |= (j.metrics & (QMIV_M_PSNR | QMIV_M_WSPSNR | QMIV_M_IVPSNR | QMIV_M_IVSSIM)) != 0;
+  }
   // order jobs by CPS variant so each variant's jobs are contiguous
   std::vector<int> order(n);
   for(int i = 0; i < n; i++) order[i] = i;
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return var[a] < var[b]; });
   std::vector<DevJob> sorted(n);
-  std::vector<int> svar(n);
-  for(int i = 0; i < n; i++) { sorted[i] = h->h_jobs[order[i]]; svar[i] = var[order[i]] < 0 ? 0 : var[order[i]]; }
+  std::vector<int> svar(n), sv(n);
+  for(int i = 0; i < n; i++) { sorted[i] = h->jobs[order[i]]; sv[i] = var[order[i]]; svar[i] = sv[i] < 0 ? 0 : sv[i]; }
   plan_grid(h, sorted.data(), n, svar);
-  // CPS bases per variant group
   int first = 0;
   while(first < n)
   {
     int last = first;
-    while(last + 1 < n && var[order[last + 1]] == var[order[first]]) last++;
+    while(last + 1 < n && sv[last + 1] == sv[first]) last++;
     int base = 0;
-    for(int i = first; i <= last; i++) { sorted[i].cps_base = base; base += (var[order[i]] < 0) ? 0 : sorted[i].cps_strips * sorted[i].cps_segs; }
+    for(int i = first; i <= last; i++) { sorted[i].cps_base = base; base += sv[i] < 0 ? 0 : sorted[i].cps_strips * sorted[i].cps_segs; }
     first = last + 1;
   }
   for(int i = 0; i < n; i++)
   {
-    if(var[order[i]] > 0 && variants()[var[order[i]]].kind == 2)
+    if(sv[i] > 0 && variants()[sv[i]].kind == 2)
     {
-      qmiv_status ts = ensure_tmaps(h, order[i], sorted[i], variants()[var[order[i]]], st);
+      qmiv_status ts = ensure_tmaps(h, sorted[i], variants()[sv[i]], st);
       if(ts != QMIV_OK) return ts;
     }
   }
-  std::memcpy(h->h_jobs, sorted.data(), sizeof(DevJob) * n);
-  CUDA_TRY(cudaMemcpyAsync(h->d_jobs, h->h_jobs, sizeof(DevJob) * n, cudaMemcpyHostToDevice, st));
+  h->jobs = sorted;
+  // SSIM family
+  h->sjobs.clear(); h->frames.clear();
+  for(int s = 0; s < 4; s++) h->steps[s].clear();
+  for(int i = 0; i < n; i++)
+    if(h->jobs[i].metrics & kSsimMetrics) { qmiv_status ps = plan_ssim(h, h->jobs[i]); if(ps != QMIV_OK) return ps; }
+  int tb = 0;
+  for(auto& s : h->sjobs) { s.tile_base = tb; tb += s.tiles_x * s.tiles_y; }
+
+  qmiv_status us = upload_tables(h, st);
+  if(us != QMIV_OK) return us;
+  const CallTables& t = h->tab;
+  const DevJob* d_jobs = reinterpret_cast<const DevJob*>(h->d_tab + t.jobs_off);
   h->prof_n = 0;
-  CUDA_TRY(prof_mark(h, "k_stats", st, true));
-  CUDA_TRY(launch_stats(h->d_jobs, h->h_jobs, n, h->params, st));
-  CUDA_TRY(prof_mark(h, "k_stats", st, false));
-  h->launches++;
+  if(any_stats)
+  {
+    CUDA_TRY(prof_mark(h, "k_stats", st, true));
+    CUDA_TRY(launch_stats(d_jobs, h->jobs.data(), n, h->params, st));
+    CUDA_TRY(prof_mark(h, "k_stats", st, false));
+    h->launches++;
+  }
   first = 0;
   while(first < n)
   {
     int last = first;
-    while(last + 1 < n && var[order[last + 1]] == var[order[first]]) last++;
-    if(var[order[first]] >= 0)
+    while(last + 1 < n && sv[last + 1] == sv[first]) last++;
+    if(sv[first] >= 0)
     {
-      const CpsVariant& cv = variants()[var[order[first]]];
+      const CpsVariant& cv = variants()[sv[first]];
       int blocks = 0;
-      for(int i = first; i <= last; i++) blocks = h->h_jobs[i].cps_base + h->h_jobs[i].cps_strips * h->h_jobs[i].cps_segs;
+      for(int i = first; i <= last; i++) blocks = h->jobs[i].cps_base + h->jobs[i].cps_strips * h->jobs[i].cps_segs;
       CUDA_TRY(prof_mark(h, cv.name, st, true));
-      if(blocks > 0) CUDA_TRY(cv.launch(h->d_jobs + first, last - first + 1, blocks, h->params, st));
+      if(blocks > 0) CUDA_TRY(cv.launch(d_jobs + first, last - first + 1, blocks, h->params, st));
       CUDA_TRY(prof_mark(h, nullptr, st, false));
       h->launches++;
     }
     first = last + 1;
   }
+  if(!h->sjobs.empty())
+  {
+    // the per-call layout puts the pyramid level tables after the SSIM jobs
+    size_t pos = t.jobs_off + align256(sizeof(DevJob) * n) + align256(sizeof(SsimJob) * h->sjobs.size());
+    for(int s = 0; s < 4; s++)
+    {
+      const PyrStep* d_steps = reinterpret_cast<const PyrStep*>(h->d_tab + pos);
+      if(!h->steps[s].empty())
+      {
+        CUDA_TRY(prof_mark(h, "k_downsample", st, true));
+        CUDA_TRY(launch_downsample(d_steps, h->steps[s].data(), (int)h->steps[s].size(), st));
+        CUDA_TRY(prof_mark(h, nullptr, st, false));
+        h->launches++;
+      }
+      pos += align256(sizeof(PyrStep) * h->steps[s].size());
+    }
+    const SsimFrame* d_frames = reinterpret_cast<const SsimFrame*>(h->d_tab + pos);
+    const SsimJob* d_sjobs = reinterpret_cast<const SsimJob*>(h->d_tab + t.jobs_off + align256(sizeof(DevJob) * n));
+    CUDA_TRY(prof_mark(h, h->opt.ssim_window == QMIV_SSIM_GAUSS11 ? "k_ssim<11>" : "k_ssim<10>", st, true));
+    CUDA_TRY(launch_ssim(d_sjobs, h->sjobs.data(), (int)h->sjobs.size(), h->opt.ssim_window, st));
+    CUDA_TRY(prof_mark(h, nullptr, st, false));
+    h->launches += 2;
+    CUDA_TRY(launch_ssim_combine(d_frames, (int)h->frames.size(), h->params, st));
+    h->launches++;
+  }
   return QMIV_OK;
+}
+
+// Window constants of the separable SSIM (the factor of the reference's coefficient table).
+cudaError_t set_ssim_constants()
+{
+  double g[11], s = 0.0;
+  for(int i = 0; i < 11; i++) { const double k = i - 5; g[i] = std::exp(-(k * k) / (2.0 * 1.5 * 1.5)); s += g[i]; }
+  float gf[11];
+  for(int i = 0; i < 11; i++) gf[i] = (float)(g[i] / s);
+  double s10 = 0.0, s11 = 0.0;
+  for(int i = 0; i < 10; i++) s10 += (double)gf[i];
+  s11 = s10 + (double)gf[10];
+  const double w0[2] = { s10 * s10, s11 * s11 };
+  return ssim_set_window_constants(gf, w0);
+}
+
+void seq_add(qmiv_handle* h, uint32_t metrics, const qmiv_frame_result* r)
+{ // xMetricStat::setPerCmpMeric / setPerPicMeric (xAppQMIV.h:245-252)
+  SeqAcc& q = h->seq;
+  if(metrics & QMIV_M_PSNR)   { for(int c = 0; c < 3; c++) q.v[c].push_back(r->psnr[c]); q.v[3].push_back(r->psnr_pic); }
+  if(metrics & QMIV_M_WSPSNR) { for(int c = 0; c < 3; c++) q.v[4 + c].push_back(r->wspsnr[c]); q.v[7].push_back(r->wspsnr_pic); }
+  if(metrics & QMIV_M_IVPSNR) q.v[8].push_back(r->ivpsnr);
+  if(metrics & QMIV_M_SSIM)   { for(int c = 0; c < 3; c++) q.v[9 + c].push_back(r->ssim[c]); q.v[12].push_back(r->ssim_pic); }
+  if(metrics & QMIV_M_MSSSIM) { for(int c = 0; c < 3; c++) q.v[13 + c].push_back(r->msssim[c]); q.v[16].push_back(r->msssim_pic); }
+  if(metrics & QMIV_M_IVSSIM) q.v[17].push_back(r->ivssim);
 }
 
 }  // namespace
@@ -495,6 +709,7 @@ void qmiv_default_options(qmiv_options* o)
   o->unnoticeable[0] = o->unnoticeable[1] = o->unnoticeable[2] = 0.01f; o->unnoticeable[3] = 0.0f;
   o->use_ws = 0; o->lon_deg = 360; o->lat_deg = 180;
   o->fake_exact = 1; o->legacy_ws8 = 0; o->ssim_window = QMIV_SSIM_REF10;
+  o->scratch_metrics = QMIV_M_ALL;
 }
 
 static qmiv_status check_options(const qmiv_options* o)
@@ -509,6 +724,7 @@ static qmiv_status check_options(const qmiv_options* o)
   if(o->cmp_w_avg[0] + o->cmp_w_avg[1] + o->cmp_w_avg[2] <= 0) return fail(QMIV_BAD_ARG, "cmp_w_avg sums to 0");
   if(o->lat_deg <= 0 || o->lat_deg > 180) return fail(QMIV_BAD_ARG, "lat_deg %d", o->lat_deg);
   if(o->ssim_window != QMIV_SSIM_REF10 && o->ssim_window != QMIV_SSIM_GAUSS11) return fail(QMIV_BAD_ARG, "ssim_window %d", o->ssim_window);
+  if(o->scratch_metrics & ~QMIV_M_ALL) return fail(QMIV_BAD_ARG, "scratch_metrics 0x%x", o->scratch_metrics);
   return QMIV_OK;
 }
 
@@ -531,32 +747,71 @@ qmiv_status qmiv_create(qmiv_handle** out, const qmiv_options* opt, int32_t max_
   auto cleanup = [&](qmiv_status st) { qmiv_destroy(h); return st; };
   if(cudaGetDevice(&h->device) != cudaSuccess) return cleanup(fail(QMIV_CUDA_ERROR, "no CUDA device"));
   cudaDeviceGetAttribute(&h->num_sms, cudaDevAttrMultiProcessorCount, h->device);
+  if(set_ssim_constants() != cudaSuccess) return cleanup(fail(QMIV_CUDA_ERROR, "SSIM window constants"));
 
-  const size_t rows_b = (size_t)max_h * 6 * sizeof(int64_t);
-  const size_t cps_b = (size_t)2 * max_h * 3 * sizeof(unsigned long long);
-  const size_t sc_b = (sizeof(JobScalars) + 255) & ~(size_t)255;
-  const size_t tm_b = 6 * 128;
-  const size_t per = ((rows_b + 255) & ~(size_t)255) + ((cps_b + 255) & ~(size_t)255) + sc_b + tm_b;
+  // per-slot scratch of the PSNR family
+  const size_t rows_b = align256((size_t)max_h * 6 * sizeof(int64_t));
+  const size_t cps_b = align256((size_t)2 * max_h * 3 * sizeof(unsigned long long));
+  const size_t sc_b = align256(sizeof(JobScalars));
+  const size_t tm_b = align256(6 * 128);
+  const size_t per = rows_b + cps_b + sc_b + tm_b;
   if(cudaMalloc(&h->slot_mem, per * max_jobs) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "slot scratch %zu B", per * max_jobs));
   if(cudaMemset(h->slot_mem, 0, per * max_jobs) != cudaSuccess) return cleanup(fail(QMIV_CUDA_ERROR, "memset"));
   h->slots.resize(max_jobs);
   for(int i = 0; i < max_jobs; i++)
   {
     uint8_t* b = (uint8_t*)h->slot_mem + per * i;
-    h->slots[i].stat_rows = (int64_t*)b; b += (rows_b + 255) & ~(size_t)255;
-    h->slots[i].cps_rows = (unsigned long long*)b; b += (cps_b + 255) & ~(size_t)255;
+    h->slots[i].stat_rows = (int64_t*)b; b += rows_b;
+    h->slots[i].cps_rows = (unsigned long long*)b; b += cps_b;
     h->slots[i].sc = (JobScalars*)b; b += sc_b;
     h->slots[i].d_tmaps = b;
   }
-  if(cudaMalloc(&h->d_jobs, sizeof(DevJob) * max_jobs) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "job table"));
-  if(cudaMallocHost(&h->h_jobs, sizeof(DevJob) * max_jobs) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "pinned job table"));
+  // per-slot scratch of the SSIM family, for the metrics the caller reserves
+  const uint32_t sm = opt->scratch_metrics;
+  size_t scp_b = 0, pyr_b = 0, part_floats = 0;
+  if(sm & QMIV_M_IVSSIM) scp_b = align256((size_t)6 * max_w * max_h * sizeof(uint16_t));
+  if(sm & QMIV_M_MSSSIM)
+    for(int sc = 1; sc <= 4; sc++) pyr_b += (size_t)6 * (max_w >> sc) * (max_h >> sc) * sizeof(uint16_t);
+  pyr_b = align256(pyr_b);
+  if(sm & kSsimMetrics)
+  {
+    const size_t full = (size_t)max_h * ssim_tiles_x(max_w);
+    part_floats = 12 * full;
+    for(int sc = 1; sc <= 4; sc++) part_floats += 3 * (size_t)(max_h >> sc) * ssim_tiles_x(max_w >> sc);
+  }
+  h->slot_partial_floats = part_floats;
+  const size_t part_b = align256(part_floats * sizeof(float) + 16);
+  const size_t vals_b = (sm & kSsimMetrics) ? align256(kSsimVals * sizeof(double)) : 0;
+  const size_t sper = scp_b + pyr_b + part_b + vals_b;
+  if(sper > 256 && (sm & kSsimMetrics))
+  {
+    if(cudaMalloc(&h->ssim_mem, sper * max_jobs) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "SSIM scratch %zu B", sper * max_jobs));
+    for(int i = 0; i < max_jobs; i++)
+    {
+      uint8_t* b = (uint8_t*)h->ssim_mem + sper * i;
+      if(scp_b) { h->slots[i].scp = (uint16_t*)b; b += scp_b; }
+      if(pyr_b) { h->slots[i].pyr = (uint16_t*)b; b += pyr_b; }
+      h->slots[i].partial = (float*)b; b += part_b;
+      h->slots[i].vals = (double*)b;
+    }
+  }
   if(cudaMalloc(&h->d_results, sizeof(qmiv_frame_result) * max_jobs) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "results"));
   if(cudaMallocHost(&h->h_results, sizeof(qmiv_frame_result) * max_jobs) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "pinned results"));
-  h->stage_elems = (size_t)max_w * max_h * 3 + 64;
-  for(int i = 0; i < 2; i++)
+  // call tables
+  CallTables& t = h->tab;
+  t.jobs_off = 0;
+  t.bytes = align256(sizeof(DevJob) * max_jobs) + align256(sizeof(SsimJob) * kSsimJobsPerFrame * max_jobs) +
+            4 * align256(sizeof(PyrStep) * kPyrStepsPerFrame * max_jobs) + align256(sizeof(SsimFrame) * max_jobs);
+  if(cudaMalloc(&h->d_tab, t.bytes) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "call tables"));
+  for(int k = 0; k < qmiv_handle::kRing; k++)
   {
-    if(cudaMalloc(&h->d_stage[i], h->stage_elems * sizeof(uint16_t)) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "staging"));
-    if(cudaMalloc(&h->d_scp[i], (size_t)max_w * max_h * 3 * sizeof(uint16_t)) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "scp"));
+    if(cudaMallocHost(&h->h_tab[k], t.bytes) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "pinned call tables"));
+    if(cudaEventCreateWithFlags(&h->tab_ev[k], cudaEventDisableTiming) != cudaSuccess) return cleanup(fail(QMIV_CUDA_ERROR, "event"));
+  }
+  for(int i = 0; i < 2; i++)
+  { // staging for host pictures: up to 3 full planes of 16-bit samples with 16-byte row pitch
+    const size_t e = (size_t)((max_w + 7) & ~7) * max_h * 3 + 64;
+    if(cudaMalloc(&h->d_stage[i], e * sizeof(uint16_t)) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "staging"));
   }
   if(cudaDeviceSynchronize() != cudaSuccess) return cleanup(fail(QMIV_CUDA_ERROR, "create sync"));
   *out = h;
@@ -567,11 +822,12 @@ qmiv_status qmiv_destroy(qmiv_handle* h)
 {
   if(!h) return QMIV_OK;
   cudaFree(h->slot_mem);
-  cudaFree(h->d_jobs);
-  cudaFreeHost(h->h_jobs);
+  cudaFree(h->ssim_mem);
   cudaFree(h->d_results);
   cudaFreeHost(h->h_results);
-  for(int i = 0; i < 2; i++) { cudaFree(h->d_stage[i]); cudaFree(h->d_scp[i]); }
+  cudaFree(h->d_tab);
+  for(int k = 0; k < qmiv_handle::kRing; k++) { cudaFreeHost(h->h_tab[k]); if(h->tab_ev[k]) cudaEventDestroy(h->tab_ev[k]); }
+  for(int i = 0; i < 2; i++) cudaFree(h->d_stage[i]);
   for(auto& kv : h->ws_cache) cudaFree(kv.second.first);
   for(auto& p : h->prof) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
   delete h;
@@ -583,6 +839,8 @@ qmiv_status qmiv_set_options(qmiv_handle* h, const qmiv_options* opt)
   if(!h) return fail(QMIV_BAD_ARG, "handle is null");
   qmiv_status s = check_options(opt);
   if(s != QMIV_OK) return s;
+  if((opt->scratch_metrics & ~h->opt.scratch_metrics) != 0)
+    return fail(QMIV_UNSUPPORTED, "scratch_metrics can only shrink after qmiv_create");
   if(opt->lat_deg != h->opt.lat_deg) { for(auto& kv : h->ws_cache) cudaFree(kv.second.first); h->ws_cache.clear(); }
   h->opt = *opt;
   derive_params(h);
@@ -593,6 +851,7 @@ int64_t qmiv_kernel_launches(const qmiv_handle* h) { return h ? h->launches : 0;
 
 int32_t qmiv_cps_variant_count(void) { return (int32_t)variants().size(); }
 const char* qmiv_cps_variant_name(int32_t v) { return (v >= 0 && v < (int32_t)variants().size()) ? variants()[v].name : ""; }
+
 qmiv_status qmiv_set_profiling(qmiv_handle* h, int32_t enable)
 {
   if(!h) return fail(QMIV_BAD_ARG, "handle is null");
@@ -628,36 +887,42 @@ qmiv_status qmiv_set_cps_variant(qmiv_handle* h, int32_t v)
 // per frame
 // ------------------------------------------------------------------------------------
 static qmiv_status frame_common(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, uint32_t metrics,
-                                const int32_t* gcd_given, uint16_t* scp0[3], uint16_t* scp1[3], int32_t scp_stride,
+                                const int32_t* gcd_given, uint16_t* const* scp0, uint16_t* const* scp1, int32_t scp_stride,
                                 qmiv_frame_result* out, cudaStream_t st)
 {
   if(!h) return fail(QMIV_BAD_ARG, "handle is null");
   qmiv_status s = check_pair(h, pic0, pic1);
   if(s != QMIV_OK) return s;
-  if(metrics & ~QMIV_M_ALL) return fail(QMIV_BAD_ARG, "metrics 0x%x", metrics);
+  if((s = check_metrics(h, metrics, pic0->width, pic0->height)) != QMIV_OK) return s;
   qmiv_pic a, b;
   if((s = upload_pic(h, pic0, 0, &a, st)) != QMIV_OK) return s;
   if((s = upload_pic(h, pic1, 1, &b, st)) != QMIV_OK) return s;
-  DevJob& j = h->h_jobs[0];
-  fill_job(h, j, &a, &b, metrics | QMIV_M_PSNR, 0);
+  h->jobs.assign(1, DevJob());
+  DevJob& j = h->jobs[0];
+  fill_job(h, j, &a, &b, metrics, 0);
   j.use_ws = h->opt.use_ws;
   if(j.use_ws) { if((s = ws_weights(h, j.H, &j.ws, &j.ws_corr)) != QMIV_OK) return s; }
-  for(int c = 0; c < 3; c++) { j.scp0[c] = scp0 ? scp0[c] : nullptr; j.scp1[c] = scp1 ? scp1[c] : nullptr; }
-  j.scp_stride = scp_stride;
+  if(scp0 && scp1) { for(int c = 0; c < 3; c++) { j.scp0[c] = scp0[c]; j.scp1[c] = scp1[c]; } j.scp_stride = scp_stride; }
+  else if(metrics & QMIV_M_IVSSIM)
+  {
+    const size_t area = (size_t)h->max_w * h->max_h;
+    for(int c = 0; c < 3; c++) { j.scp0[c] = h->slots[0].scp + c * area; j.scp1[c] = h->slots[0].scp + (3 + c) * area; }
+    j.scp_stride = j.W;
+  }
   if(gcd_given)
   {
-    JobScalars tmp;
-    std::memset(&tmp, 0, sizeof(tmp));
-    for(int c = 0; c < 3; c++) tmp.gcd[c] = gcd_given[c];
-    CUDA_TRY(cudaMemcpyAsync(h->slots[0].sc->gcd, tmp.gcd, sizeof(tmp.gcd), cudaMemcpyHostToDevice, st));
+    int32_t g[4] = { gcd_given[0], gcd_given[1], gcd_given[2], 0 };
+    CUDA_TRY(cudaMemcpyAsync(h->slots[0].sc->gcd, g, sizeof(g), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaStreamSynchronize(st)); // `g` lives on this stack frame
     j.gcd_given = 1;
   }
   CUDA_TRY(cudaMemsetAsync(h->d_results, 0, sizeof(qmiv_frame_result), st));
-  if((s = run_psnr_family(h, 1, st)) != QMIV_OK) return s;
+  if((s = run_jobs(h, st)) != QMIV_OK) return s;
   CUDA_TRY(cudaMemcpyAsync(h->h_results, h->d_results, sizeof(qmiv_frame_result), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaStreamSynchronize(st));
   *out = h->h_results[0];
   out->metrics = metrics;
+  if(out->status != QMIV_OK) return fail((qmiv_status)out->status, "device-side wait gave up");
   return QMIV_OK;
 }
 
@@ -665,24 +930,9 @@ qmiv_status qmiv_calc_frame(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic
                             qmiv_frame_result* out, qmiv_stream stream)
 {
   if(!out) return fail(QMIV_BAD_ARG, "out is null");
-  cudaStream_t st = (cudaStream_t)stream;
-  const bool need_scp = (metrics & QMIV_M_IVSSIM) != 0;
-  uint16_t* s0[3] = { nullptr, nullptr, nullptr };
-  uint16_t* s1[3] = { nullptr, nullptr, nullptr };
-  int32_t sstride = 0;
-  if(need_scp && pic0)
-  {
-    const size_t area = (size_t)pic0->width * pic0->height;
-    for(int c = 0; c < 3; c++) { s0[c] = h->d_scp[0] + c * area; s1[c] = h->d_scp[1] + c * area; }
-    sstride = pic0->width;
-  }
-  qmiv_status s = frame_common(h, pic0, pic1, metrics, nullptr, need_scp ? s0 : nullptr, need_scp ? s1 : nullptr, sstride, out, st);
+  qmiv_status s = frame_common(h, pic0, pic1, metrics, nullptr, nullptr, nullptr, 0, out, (cudaStream_t)stream);
   if(s != QMIV_OK) return s;
-  // sequence statistics (xMetricStat::setPerCmpMeric / setPerPicMeric)
-  SeqAcc& q = h->seq;
-  if(metrics & QMIV_M_PSNR)   { for(int c = 0; c < 3; c++) q.v[c].push_back(out->psnr[c]);   q.v[3].push_back(out->psnr_pic); }
-  if(metrics & QMIV_M_WSPSNR) { for(int c = 0; c < 3; c++) q.v[4 + c].push_back(out->wspsnr[c]); q.v[7].push_back(out->wspsnr_pic); }
-  if(metrics & QMIV_M_IVPSNR) q.v[8].push_back(out->ivpsnr);
+  seq_add(h, metrics, out);
   return QMIV_OK;
 }
 
@@ -720,33 +970,27 @@ qmiv_status qmiv_ivpsnr(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pi
 qmiv_status qmiv_scp(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, const int32_t* gcd,
                      uint16_t* scp0[3], uint16_t* scp1[3], int32_t scp_stride, int32_t scp_is_device, qmiv_stream stream)
 {
+  if(!h) return fail(QMIV_BAD_ARG, "handle is null");
   if(!scp0 || !scp1) return fail(QMIV_BAD_ARG, "scp outputs are null");
   for(int c = 0; c < 3; c++) if(!scp0[c] || !scp1[c]) return fail(QMIV_BAD_ARG, "scp plane %d is null", c);
   if(!pic0) return fail(QMIV_BAD_ARG, "pic0 is null");
   if(scp_stride < pic0->width) return fail(QMIV_BAD_ARG, "scp_stride %d < width %d", scp_stride, pic0->width);
   cudaStream_t st = (cudaStream_t)stream;
-  uint16_t* d0[3]; uint16_t* d1[3];
-  const size_t area = (size_t)pic0->width * pic0->height;
-  int32_t dstride = scp_stride;
-  if(scp_is_device) { for(int c = 0; c < 3; c++) { d0[c] = scp0[c]; d1[c] = scp1[c]; } }
-  else
-  {
-    if(pic0->width > h->max_w || pic0->height > h->max_h) return fail(QMIV_TOO_LARGE, "picture too large");
-    for(int c = 0; c < 3; c++) { d0[c] = h->d_scp[0] + c * area; d1[c] = h->d_scp[1] + c * area; }
-    dstride = pic0->width;
-  }
   qmiv_frame_result r;
-  qmiv_status s = frame_common(h, pic0, pic1, QMIV_M_IVSSIM, gcd, d0, d1, dstride, &r, st);
+  // the SCP pictures come out of the CPS kernel, which runs for IV-PSNR
+  if(scp_is_device) return frame_common(h, pic0, pic1, QMIV_M_IVPSNR, gcd, scp0, scp1, scp_stride, &r, st);
+  if(!h->slots[0].scp) return fail(QMIV_UNSUPPORTED, "host SCP outputs need IV-SSIM scratch (scratch_metrics)");
+  const size_t area = (size_t)h->max_w * h->max_h;
+  uint16_t* d0[3]; uint16_t* d1[3];
+  for(int c = 0; c < 3; c++) { d0[c] = h->slots[0].scp + c * area; d1[c] = h->slots[0].scp + (3 + c) * area; }
+  qmiv_status s = frame_common(h, pic0, pic1, QMIV_M_IVPSNR, gcd, d0, d1, pic0->width, &r, st);
   if(s != QMIV_OK) return s;
-  if(!scp_is_device)
+  for(int c = 0; c < 3; c++)
   {
-    for(int c = 0; c < 3; c++)
-    {
-      CUDA_TRY(cudaMemcpy2DAsync(scp0[c], (size_t)scp_stride * 2, d0[c], (size_t)dstride * 2, (size_t)pic0->width * 2, pic0->height, cudaMemcpyDeviceToHost, st));
-      CUDA_TRY(cudaMemcpy2DAsync(scp1[c], (size_t)scp_stride * 2, d1[c], (size_t)dstride * 2, (size_t)pic0->width * 2, pic0->height, cudaMemcpyDeviceToHost, st));
-    }
-    CUDA_TRY(cudaStreamSynchronize(st));
+    CUDA_TRY(cudaMemcpy2DAsync(scp0[c], (size_t)scp_stride * 2, d0[c], (size_t)pic0->width * 2, (size_t)pic0->width * 2, pic0->height, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpy2DAsync(scp1[c], (size_t)scp_stride * 2, d1[c], (size_t)pic0->width * 2, (size_t)pic0->width * 2, pic0->height, cudaMemcpyDeviceToHost, st));
   }
+  CUDA_TRY(cudaStreamSynchronize(st));
   return QMIV_OK;
 }
 
@@ -757,23 +1001,84 @@ qmiv_status qmiv_calc_batch(qmiv_handle* h, const qmiv_job* jobs, int32_t n, qmi
   if(n > h->max_jobs) return fail(QMIV_TOO_LARGE, "%d jobs > max_jobs %d", n, h->max_jobs);
   if(!results) return fail(QMIV_BAD_ARG, "results is null");
   cudaStream_t st = (cudaStream_t)stream;
+  h->jobs.assign(n, DevJob());
   for(int i = 0; i < n; i++)
   {
     const qmiv_job& jb = jobs[i];
     qmiv_status s = check_pair(h, &jb.pic0, &jb.pic1);
     if(s != QMIV_OK) return fail(s, "job %d: %s", i, g_last_error.c_str());
     if(!jb.pic0.is_device) return fail(QMIV_BAD_ARG, "job %d: batch pictures must be device pointers", i);
-    if(jb.metrics & ~QMIV_M_ALL) return fail(QMIV_BAD_ARG, "job %d: metrics 0x%x", i, jb.metrics);
-    if(jb.metrics & (QMIV_M_SSIM | QMIV_M_MSSSIM | QMIV_M_IVSSIM)) return fail(QMIV_UNSUPPORTED, "job %d: SSIM metrics in batches", i);
-    DevJob& j = h->h_jobs[i];
-    fill_job(h, j, &jb.pic0, &jb.pic1, jb.metrics | QMIV_M_PSNR, i);
+    if((s = check_metrics(h, jb.metrics, jb.pic0.width, jb.pic0.height)) != QMIV_OK) return fail(s, "job %d: %s", i, g_last_error.c_str());
+    DevJob& j = h->jobs[i];
+    fill_job(h, j, &jb.pic0, &jb.pic1, jb.metrics, i);
     j.result = results + i;
     j.use_ws = jb.use_ws;
     if(j.use_ws) { s = ws_weights(h, j.H, &j.ws, &j.ws_corr); if(s != QMIV_OK) return s; }
-    for(int c = 0; c < 3; c++) { j.scp0[c] = jb.scp0[c]; j.scp1[c] = jb.scp1[c]; }
-    j.scp_stride = jb.scp_stride;
+    if(jb.scp0[0] && jb.scp1[0]) { for(int c = 0; c < 3; c++) { j.scp0[c] = jb.scp0[c]; j.scp1[c] = jb.scp1[c]; } j.scp_stride = jb.scp_stride; }
+    else if(jb.metrics & QMIV_M_IVSSIM)
+    {
+      const size_t area = (size_t)h->max_w * h->max_h;
+      for(int c = 0; c < 3; c++) { j.scp0[c] = h->slots[i].scp + c * area; j.scp1[c] = h->slots[i].scp + (3 + c) * area; }
+      j.scp_stride = j.W;
+    }
   }
-  return run_psnr_family(h, n, st);
+  return run_jobs(h, st);
+}
+
+qmiv_status qmiv_ssim(qmiv_handle* h, const qmiv_pic* tst, const qmiv_pic* ref, int32_t calc_l, double ssim[4], qmiv_stream stream)
+{ // xSSIM::calcPicSSIM(Tst, Ref, CalcL) on any two pictures, no other metric
+  if(!h) return fail(QMIV_BAD_ARG, "handle is null");
+  if(!ssim) return fail(QMIV_BAD_ARG, "ssim is null");
+  qmiv_status s = check_pair(h, tst, ref);
+  if(s != QMIV_OK) return s;
+  if(!h->slots[0].vals) return fail(QMIV_UNSUPPORTED, "SSIM needs SSIM scratch (scratch_metrics)");
+  cudaStream_t st = (cudaStream_t)stream;
+  qmiv_pic a, b;
+  if((s = upload_pic(h, tst, 0, &a, st)) != QMIV_OK) return s;
+  if((s = upload_pic(h, ref, 1, &b, st)) != QMIV_OK) return s;
+  const int cs = a.chroma_format == QMIV_CF420 ? 1 : 0, sb = a.sample_bytes;
+  h->jobs.clear(); h->sjobs.clear(); h->frames.clear();
+  for(int k = 0; k < 4; k++) h->steps[k].clear();
+  float* part = h->slots[0].partial;
+  for(int c = 0; c < 3; c++)
+    add_ssim_job(h, plane_of(a.plane[c], a.stride[c], sb, c ? cs : 0), plane_of(b.plane[c], b.stride[c], sb, c ? cs : 0),
+                 a.width, a.height, a.bitdepth, calc_l ? 1 : 0, part, h->slots[0].vals + c);
+  int tb = 0;
+  for(auto& sj : h->sjobs) { sj.tile_base = tb; tb += sj.tiles_x * sj.tiles_y; }
+  if((s = upload_tables(h, st)) != QMIV_OK) return s;
+  // no picture-pair jobs in this call: the SSIM jobs start the table
+  const SsimJob* d_sjobs = reinterpret_cast<const SsimJob*>(h->d_tab + h->tab.jobs_off);
+  h->prof_n = 0;
+  CUDA_TRY(launch_ssim(d_sjobs, h->sjobs.data(), 3, h->opt.ssim_window, st));
+  h->launches += 2;
+  double v[3];
+  CUDA_TRY(cudaMemcpyAsync(v, h->slots[0].vals, sizeof(v), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  for(int c = 0; c < 3; c++) ssim[c] = v[c];
+  ssim[3] = 0.0;
+  return QMIV_OK;
+}
+
+qmiv_status qmiv_msssim(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, double msssim[4], qmiv_stream stream)
+{
+  if(!msssim) return fail(QMIV_BAD_ARG, "msssim is null");
+  qmiv_frame_result r;
+  qmiv_status s = frame_common(h, pic0, pic1, QMIV_M_MSSSIM, nullptr, nullptr, nullptr, 0, &r, (cudaStream_t)stream);
+  if(s != QMIV_OK) return s;
+  for(int c = 0; c < 4; c++) msssim[c] = r.msssim[c];
+  return QMIV_OK;
+}
+
+qmiv_status qmiv_ivssim(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, const int32_t* gcd,
+                        double* iv, double* r2t, double* t2r, qmiv_stream stream)
+{
+  qmiv_frame_result r;
+  qmiv_status s = frame_common(h, pic0, pic1, QMIV_M_IVSSIM, gcd, nullptr, nullptr, 0, &r, (cudaStream_t)stream);
+  if(s != QMIV_OK) return s;
+  if(iv) *iv = r.ivssim;
+  if(r2t) *r2t = r.ivssim_r2t;
+  if(t2r) *t2r = r.ivssim_t2r;
+  return QMIV_OK;
 }
 
 qmiv_status qmiv_finish_sequence(qmiv_handle* h, qmiv_seq_result* out)
@@ -793,14 +1098,21 @@ qmiv_status qmiv_finish_sequence(qmiv_handle* h, qmiv_seq_result* out)
   };
   const SeqAcc& q = h->seq;
   size_t nf = 0;
-  for(int k = 0; k < 16; k++) nf = std::max(nf, q.v[k].size());
+  for(int k = 0; k < 18; k++) nf = std::max(nf, q.v[k].size());
   out->num_frames = (int32_t)nf;
-  for(int c = 0; c < 3; c++) { out->psnr[c] = avg(q.v[c]); out->wspsnr[c] = avg(q.v[4 + c]); out->ssim[c] = avg(q.v[9 + c]); out->msssim[c] = avg(q.v[13 + c]); }
+  for(int c = 0; c < 3; c++)
+  {
+    out->psnr[c] = avg(q.v[c]); out->wspsnr[c] = avg(q.v[4 + c]);
+    out->ssim[c] = avg(q.v[9 + c]); out->msssim[c] = avg(q.v[13 + c]);
+  }
   out->psnr_pic = avg(q.v[3]); out->wspsnr_pic = avg(q.v[7]); out->ivpsnr = avg(q.v[8]);
-  out->ssim_pic = avg(q.v[12]);
+  out->ssim_pic = avg(q.v[12]); out->msssim_pic = avg(q.v[16]); out->ivssim = avg(q.v[17]);
   if(!q.v[3].empty()) out->metrics |= QMIV_M_PSNR;
   if(!q.v[7].empty()) out->metrics |= QMIV_M_WSPSNR;
   if(!q.v[8].empty()) out->metrics |= QMIV_M_IVPSNR;
+  if(!q.v[12].empty()) out->metrics |= QMIV_M_SSIM;
+  if(!q.v[16].empty()) out->metrics |= QMIV_M_MSSSIM;
+  if(!q.v[17].empty()) out->metrics |= QMIV_M_IVSSIM;
   return QMIV_OK;
 }
 
@@ -810,14 +1122,5 @@ qmiv_status qmiv_reset_sequence(qmiv_handle* h)
   for(auto& v : h->seq.v) v.clear();
   return QMIV_OK;
 }
-
-// SSIM family: provided by the SSIM translation unit once built; until then these report
-// UNSUPPORTED so callers fail loudly instead of silently skipping work.
-qmiv_status qmiv_ssim(qmiv_handle* h, const qmiv_pic*, const qmiv_pic*, int32_t, double*, qmiv_stream)
-{ return h ? fail(QMIV_UNSUPPORTED, "SSIM not built") : fail(QMIV_BAD_ARG, "handle is null"); }
-qmiv_status qmiv_msssim(qmiv_handle* h, const qmiv_pic*, const qmiv_pic*, double*, qmiv_stream)
-{ return h ? fail(QMIV_UNSUPPORTED, "MS-SSIM not built") : fail(QMIV_BAD_ARG, "handle is null"); }
-qmiv_status qmiv_ivssim(qmiv_handle* h, const qmiv_pic*, const qmiv_pic*, const int32_t*, double*, double*, double*, qmiv_stream)
-{ return h ? fail(QMIV_UNSUPPORTED, "IV-SSIM not built") : fail(QMIV_BAD_ARG, "handle is null"); }
 
 }  // extern "C"

@@ -33,6 +33,7 @@ struct DevJob {
   uint16_t* scp1[3];                  // built from picture 1 (R2T argmin), may be null
   int32_t scp_stride;
   int32_t gcd_given;                  // 1: sc->gcd preset by the host, stats kernel leaves it
+  int32_t slot;                       // the handle's scratch slot (host bookkeeping)
   const void* tmaps;                  // 6 tensor maps (picture 0 Y,Cb,Cr then picture 1) or null
   int64_t* stat_rows;                 // [H][6]: sum(P1-P0)[3], sum((P1-P0)^2)[3]
   unsigned long long* cps_rows;       // [2][H][3]: per-row CPS SSE, direction R2T then T2R

@@ -1,0 +1,57 @@
+// Device descriptors of the SSIM-family kernels (k_ssim.cu) and their host launchers.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "qmiv_internal.h"
+
+namespace qmiv {
+
+// A plane read as sample(x, y) = ptr[(y >> shift) * stride + (x >> shift)]: shift 1 reads a 4:2:0
+// chroma plane at luma resolution (nearest-neighbour upsampling, xPixelOpsSTD.cpp:30-49).
+struct SsimPlane {
+  const void* ptr;
+  int32_t stride;
+  int8_t sbytes;
+  int8_t shift;
+  int16_t pad;
+};
+
+// One SSIM evaluation of a plane pair (xSSIM::xCalcCmpSSIM, xSSIM.cpp:91-112).
+struct SsimJob {
+  SsimPlane a, b;        // a = "Tst", b = "Ref" of calcPicSSIM; b also gives the centring offset
+  int32_t W, H;
+  int32_t calc_l;        // 0: contrast-structure only (MS-SSIM scales 0 and 4)
+  float c1, c2;          // (0.01 Max)^2, (0.03 Max)^2
+  int32_t tiles_x, tiles_y, tile_base;
+  float* partial;        // [(H-10)][tiles_x] per-tile row sums
+  double* out;           // picture mean
+};
+
+// One DownsampleHV step of the MS-SSIM pyramid.
+struct PyrStep {
+  SsimPlane src;
+  uint16_t* dst;
+  int32_t dst_stride, dw, dh;
+};
+
+// Per frame: where the SSIM-job values are and which metrics to combine.
+// vals: [0..2] SSIM, [3..17] MS-SSIM scale i component c at 3+3i+c, [18..20] IV-SSIM T2R
+// (picture 0 vs SCP1), [21..23] IV-SSIM R2T (picture 1 vs SCP0).
+struct SsimFrame {
+  uint32_t metrics;
+  int32_t pad;
+  qmiv_frame_result* result;
+  const double* vals;
+};
+
+constexpr int kSsimVals = 24;
+
+cudaError_t ssim_set_window_constants(const float g[11], const double w0[2]);
+int ssim_tiles_x(int W);
+int ssim_tiles_y(int H);
+cudaError_t launch_ssim(const SsimJob* d_jobs, const SsimJob* h_jobs, int n, int window, cudaStream_t st);
+cudaError_t launch_downsample(const PyrStep* d_steps, const PyrStep* h_steps, int n, cudaStream_t st);
+cudaError_t launch_ssim_combine(const SsimFrame* d_frames, int n, const Params& p, cudaStream_t st);
+
+}  // namespace qmiv

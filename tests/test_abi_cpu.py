@@ -48,7 +48,7 @@ def test_defaults_match_reference(lib):
     assert list(o.cmp_w_search) == [4, 1, 1, 0]      # xCorrespPixelShift.h:33
     assert list(o.cmp_w_avg) == [4, 1, 1, 0]
     assert [round(x, 6) for x in o.unnoticeable] == [0.01, 0.01, 0.01, 0.0]  # xGlobClrDiff.h:20
-    assert (o.lon_deg, o.lat_deg, o.fake_exact, o.legacy_ws8, o.use_ws) == (360, 180, 1, 0, 0)
+    assert (o.lon_deg, o.lat_deg, o.fake_exact, o.legacy_ws8, o.use_ws, o.scratch_metrics) == (360, 180, 1, 0, 0, 63)
 
 
 def test_status_strings_and_version(lib):
