@@ -173,6 +173,70 @@ def cpu_baseline_sample():
             "sample": "2 of 96 picture pairs (4096x2048 ERP + 1920x1080), GCD+PSNR+WS-PSNR+IV-PSNR, oracle/ C port"}
 
 
+SSIM_WORKLOAD = "ivssim-ssim-msssim-10bit-420: 17 frames 1920x1080, drifting block shifts, SR 2, REF10 window"
+
+
+def ssim_workload(args, dev, stream):
+    """IV-SSIM + SSIM + MS-SSIM over 17 frames of 1920x1080 10-bit 4:2:0, one batched call per step
+    (device-resident inputs), and the same through one qmiv_calc_frame per frame."""
+    import ctypes as C
+
+    import torch
+
+    import ivpsnr_gb300 as q
+    from ivpsnr_gb300 import _abi, synth
+    w, h, nf = 1920, 1080, 17
+    bufs, qjobs = [], []
+    for f in range(nf):
+        ref, tst = synth.pair420(w, h, BD, seed=synth.seed_for(2, 0, f), drift=True, shift_seed=synth.seed_for(2, 0, 0), frame=f)
+        d0, d1 = torch.from_numpy(ref.view(np.int16)).to(dev), torch.from_numpy(tst.view(np.int16)).to(dev)
+        bufs.append((d0, d1))
+        a = w * h
+        ca = a // 4
+        pl = lambda t: [t[:a].view(h, w), t[a:a + ca].view(h // 2, w // 2), t[a + ca:].view(h // 2, w // 2)]
+        j = _abi.Job()
+        j.pic0 = q.make_pic(pl(d0), BD)
+        j.pic1 = q.make_pic(pl(d1), BD)
+        j.metrics = q.M_SSIM | q.M_MSSSIM | q.M_IVSSIM
+        qjobs.append(j)
+    rsz = C.sizeof(_abi.FrameResult)
+    res = torch.zeros(nf * rsz, dtype=torch.uint8, device=dev)
+    metrics = q.M_SSIM | q.M_MSSSIM | q.M_IVSSIM
+    P = q.Processor(w, h, max_jobs=nf, scratch_metrics=metrics)
+    sptr = stream.cuda_stream
+    for _ in range(args.warmup):
+        P.calc_batch(qjobs, res.data_ptr(), sptr)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        P.calc_batch(qjobs, res.data_ptr(), sptr)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    P.set_profiling(True)
+    P.calc_batch(qjobs, res.data_ptr(), sptr)
+    kt = {}
+    for n, t in P.kernel_times():
+        kt[n] = kt.get(n, 0.0) + t
+    P.set_profiling(False)
+    r0 = _abi.FrameResult.from_buffer_copy(bytes(res[:rsz].cpu().numpy()))
+    P.close()
+    Pp = q.Processor(w, h, max_jobs=1, scratch_metrics=metrics)
+    for (j) in qjobs[:2]:
+        Pp.calc_frame(j.pic0, j.pic1, metrics, sptr)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for j in qjobs:
+        Pp.calc_frame(j.pic0, j.pic1, metrics, sptr)
+    plain_ms = (time.perf_counter() - t) * 1e3
+    Pp.close()
+    px = w * h * nf
+    return {"workload": SSIM_WORKLOAD, "value": px / (ms * 1e-3) / 1e9, "unit": "Gpixel/s", "ms_per_step": ms,
+            "plain_value": px / (plain_ms * 1e-3) / 1e9, "batched_over_plain": plain_ms / ms, "kernel_ms": kt,
+            "check": {"ivssim_frame0": r0.ivssim, "ssim_frame0": list(r0.ssim)[:3]}}
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -211,7 +275,8 @@ def run_ours(args):
     rsz = ctypes.sizeof(_abi.FrameResult)
     res_dev = torch.zeros(nres * rsz, dtype=torch.uint8, device=dev)
     res_host = torch.zeros(nres * rsz, dtype=torch.uint8, pin_memory=True)
-    P = q.Processor(4096, 2048, max_jobs=nres)
+    PSNRS = q.M_PSNR | q.M_WSPSNR | q.M_IVPSNR
+    P = q.Processor(4096, 2048, max_jobs=nres, scratch_metrics=PSNRS)
     stream = torch.cuda.current_stream(dev)
     sptr = stream.cuda_stream
 
@@ -284,9 +349,9 @@ def run_ours(args):
     int_peak = 152 * 128 * sm_mhz * 1e6  # INT32 lanes x clock (derived from the sampled clock)
 
     # ---- plain per-frame form: one qmiv_calc_frame per pair (device inputs) ----
-    Pp = q.Processor(4096, 2048, max_jobs=1)
+    Pp = q.Processor(4096, 2048, max_jobs=1, scratch_metrics=PSNRS)
     plain_pics = [(j.pic0, j.pic1, erp) for j, (_, _, _, _, erp) in zip(qjobs, jobs)]
-    Pws = q.Processor(4096, 2048, max_jobs=1, use_ws=True)
+    Pws = q.Processor(4096, 2048, max_jobs=1, use_ws=True, scratch_metrics=PSNRS)
     def plain_pass():
         for p0, p1, erp in plain_pics:
             (Pws if erp else Pp).calc_frame(p0, p1, q.M_PSNR | q.M_WSPSNR | q.M_IVPSNR, sptr)
@@ -317,6 +382,13 @@ def run_ours(args):
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1) / args.steps
     e2e_value = px_per_step * world / (e2e_ms * 1e-3) / 1e9
+    P.close()
+    Pp.close()
+    Pws.close()
+    del devbufs, host
+    torch.cuda.empty_cache()
+
+    ssim_line = None if args.skip_ssim else ssim_workload(args, dev, stream)
 
     if rank == 0:
         line = {
@@ -340,12 +412,11 @@ def run_ours(args):
             "plain": {"value": plain_value, "unit": "Gpixel/s", "batched_over_plain": value / world / plain_value},
             "check": {"ivpsnr_pair0": r0.ivpsnr, "gcd_pair0": list(r0.gcd_r2t)[:3]},
         }
+        if ssim_line:
+            line["ivssim"] = ssim_line
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_sample()
         print(json.dumps(line))
-    P.close()
-    Pp.close()
-    Pws.close()
     if world > 1:
         dist.destroy_process_group()
 
@@ -359,6 +430,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="multiview", choices=["multiview", "small"],
                     help="small: the 24-pair 1080p case used for ncu captures")
+    ap.add_argument("--skip-ssim", action="store_true", help="skip the IV-SSIM / SSIM / MS-SSIM workload")
     ap.add_argument("--kernels-only", action="store_true",
                     help="time only the batched launches (for profiler captures)")
     args = ap.parse_args()
