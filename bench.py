@@ -249,6 +249,11 @@ def run_ours(args):
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.workload == "ssim":
+        r = ssim_workload(args, dev, torch.cuda.current_stream(dev))
+        if rank == 0:
+            print(json.dumps(r))
+        return
     jobs = jobs_list(args.workload == "small")
     host = make_inputs(jobs)
     devbufs = []
@@ -428,7 +433,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="multiview", choices=["multiview", "small"],
+    ap.add_argument("--workload", default="multiview", choices=["multiview", "small", "ssim"],
                     help="small: the 24-pair 1080p case used for ncu captures")
     ap.add_argument("--skip-ssim", action="store_true", help="skip the IV-SSIM / SSIM / MS-SSIM workload")
     ap.add_argument("--kernels-only", action="store_true",
