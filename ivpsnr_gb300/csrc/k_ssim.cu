@@ -29,7 +29,15 @@ __constant__ double c_omd[2];
 
 namespace {
 
-constexpr int kTX = 32, kTY = 32, kThreads = 256;
+constexpr int kTX = 32, kThreads = 256, kIH = 64;  // staged rows: output rows + window - 1
+template <int WIN> struct SGeo {
+  static constexpr int TY = kIH - WIN + 1;          // 55 output rows (REF10), 54 (GAUSS11)
+  static constexpr int IW = kTX + WIN - 1;          // staged columns
+  static constexpr int RS = ((IW + 2) / 4) * 4 + 1; // row stride = 1 (mod 4): conflict-free h-pass reads
+  static constexpr int HS = kTX + 1;                // h-moment row stride (= 1 mod 4)
+  static constexpr int RPT = (TY + 7) / 8;          // output rows per thread in the v-pass
+  static constexpr int SMEM = (2 * kIH * RS + 5 * kIH * HS) * 4;
+};
 
 __device__ __forceinline__ int ld_plane(const SsimPlane& p, int x, int y)
 {
@@ -44,12 +52,38 @@ __device__ __forceinline__ int find_ssim_job(const SsimJob* __restrict__ jobs, i
   return lo;
 }
 
+// Stage one plane's rows (warp per row, lanes along x) as centred floats; rows and columns past
+// the picture clamp (they only feed outputs outside the valid region).
+template <typename T, int SH, int IW, int RS>
+__device__ __forceinline__ void stage_rows(const SsimPlane& P, float* dst, int x0, int y0, int W, int H, int c)
+{
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for(int r = warp; r < kIH; r += kThreads / 32)
+  {
+    const int gy = min(y0 - 5 + r, H - 1);
+    const T* row = reinterpret_cast<const T*>(P.ptr) + (int64_t)(gy >> SH) * P.stride;
+    for(int q = lane; q < IW; q += 32)
+    {
+      const int gx = min(x0 - 5 + q, W - 1);
+      dst[r * RS + q] = (float)((int)__ldg(row + (gx >> SH)) - c);
+    }
+  }
+}
+
+template <int IW, int RS>
+__device__ __forceinline__ void stage_plane(const SsimPlane& P, float* dst, int x0, int y0, int W, int H, int c)
+{
+  if(P.sbytes == 1) { if(P.shift) stage_rows<uint8_t, 1, IW, RS>(P, dst, x0, y0, W, H, c); else stage_rows<uint8_t, 0, IW, RS>(P, dst, x0, y0, W, H, c); }
+  else              { if(P.shift) stage_rows<uint16_t, 1, IW, RS>(P, dst, x0, y0, W, H, c); else stage_rows<uint16_t, 0, IW, RS>(P, dst, x0, y0, W, H, c); }
+}
+
 template <int WIN>
 __global__ void __launch_bounds__(kThreads) k_ssim(const SsimJob* __restrict__ jobs, int njobs)
 {
-  constexpr int IW = kTX + WIN - 1, IH = kTY + WIN - 1;   // staged input tile
-  __shared__ float s_in[2][IH][IW + 1];
-  __shared__ float s_h[5][IH][kTX + 1];
+  using G = SGeo<WIN>;
+  extern __shared__ float smem[];
+  float* s_in = smem;                       // [2][kIH][RS]
+  float* s_h = smem + 2 * kIH * G::RS;      // [5][kIH][HS]
   __shared__ int s_c;
 
   const int jb = find_ssim_job(jobs, njobs, blockIdx.x);
@@ -57,29 +91,30 @@ __global__ void __launch_bounds__(kThreads) k_ssim(const SsimJob* __restrict__ j
   const int local = blockIdx.x - J.tile_base;
   const int ty = local / J.tiles_x, tx = local - ty * J.tiles_x;
   const int W = J.W, H = J.H;
-  const int x0 = 5 + tx * kTX, y0 = 5 + ty * kTY;
-  const int x1 = min(x0 + kTX, W - 5), y1 = min(y0 + kTY, H - 5);
-  const int tid = threadIdx.x;
+  const int x0 = 5 + tx * kTX, y0 = 5 + ty * G::TY;
+  const int x1 = min(x0 + kTX, W - 5), y1 = min(y0 + G::TY, H - 5);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   if(tid == 0) s_c = ld_plane(J.b, min((x0 + x1) >> 1, W - 1), min((y0 + y1) >> 1, H - 1));
   __syncthreads();
   const int c = s_c;
-  for(int i = tid; i < IH * IW; i += kThreads)
-  {
-    const int r = i / IW, q = i - r * IW;
-    const int gx = min(x0 - 5 + q, W - 1), gy = min(y0 - 5 + r, H - 1);
-    s_in[0][r][q] = (float)(ld_plane(J.a, gx, gy) - c);
-    s_in[1][r][q] = (float)(ld_plane(J.b, gx, gy) - c);
-  }
+  stage_plane<G::IW, G::RS>(J.a, s_in, x0, y0, W, H, c);
+  stage_plane<G::IW, G::RS>(J.b, s_in + kIH * G::RS, x0, y0, W, H, c);
   __syncthreads();
 
-  // horizontal pass: 4 consecutive output columns of one input row per work item
-  for(int item = tid; item < IH * (kTX / 4); item += kThreads)
+  // horizontal pass: item = (row, 4 consecutive output columns); 8 items per row
+  #pragma unroll 1
+  for(int item = tid; item < kIH * (kTX / 4); item += kThreads)
   {
-    const int r = item / (kTX / 4), q0 = (item - r * (kTX / 4)) * 4;
-    float a[4 + WIN - 1], b[4 + WIN - 1];
+    const int r = item >> 3, q0 = (item & 7) * 4;
+    float a[4 + WIN - 1], b[4 + WIN - 1], aa[4 + WIN - 1], bb[4 + WIN - 1], ab[4 + WIN - 1];
     #pragma unroll
-    for(int i = 0; i < 4 + WIN - 1; i++) { a[i] = s_in[0][r][q0 + i]; b[i] = s_in[1][r][q0 + i]; }
+    for(int i = 0; i < 4 + WIN - 1; i++)
+    {
+      a[i] = s_in[r * G::RS + q0 + i];
+      b[i] = s_in[kIH * G::RS + r * G::RS + q0 + i];
+      aa[i] = a[i] * a[i]; bb[i] = b[i] * b[i]; ab[i] = a[i] * b[i];
+    }
     #pragma unroll
     for(int o = 0; o < 4; o++)
     {
@@ -87,33 +122,31 @@ __global__ void __launch_bounds__(kThreads) k_ssim(const SsimJob* __restrict__ j
       #pragma unroll
       for(int k = 0; k < WIN; k++)
       {
-        const float g = c_g[k], av = a[o + k], bv = b[o + k];
-        const float ga = g * av, gb = g * bv;
-        m0 += ga; m1 += gb;
-        m2 = fmaf(ga, av, m2); m3 = fmaf(gb, bv, m3); m4 = fmaf(ga, bv, m4);
+        const float g = c_g[k];
+        m0 = fmaf(g, a[o + k], m0); m1 = fmaf(g, b[o + k], m1);
+        m2 = fmaf(g, aa[o + k], m2); m3 = fmaf(g, bb[o + k], m3); m4 = fmaf(g, ab[o + k], m4);
       }
-      s_h[0][r][q0 + o] = m0; s_h[1][r][q0 + o] = m1; s_h[2][r][q0 + o] = m2;
-      s_h[3][r][q0 + o] = m3; s_h[4][r][q0 + o] = m4;
+      float* h = s_h + r * G::HS + q0 + o;
+      h[0] = m0; h[kIH * G::HS] = m1; h[2 * kIH * G::HS] = m2; h[3 * kIH * G::HS] = m3; h[4 * kIH * G::HS] = m4;
     }
   }
   __syncthreads();
 
-  // vertical pass: one column, 4 output rows per thread
-  const int col = tid & 31, rg = tid >> 5;                 // 8 row groups of 4 rows
-  float acc[4][5];
+  // vertical pass: lane = column, warp = RPT consecutive output rows
+  float acc[G::RPT][5];
   #pragma unroll
-  for(int o = 0; o < 4; o++)
+  for(int o = 0; o < G::RPT; o++)
     #pragma unroll
     for(int m = 0; m < 5; m++) acc[o][m] = 0.f;
   #pragma unroll
-  for(int i = 0; i < 4 + WIN - 1; i++)
+  for(int i = 0; i < G::RPT + WIN - 1; i++)
   {
-    const int r = rg * 4 + i;
+    const int r = min(warp * G::RPT + i, kIH - 1);
     float hv[5];
     #pragma unroll
-    for(int m = 0; m < 5; m++) hv[m] = s_h[m][r][col];
+    for(int m = 0; m < 5; m++) hv[m] = s_h[m * kIH * G::HS + r * G::HS + lane];
     #pragma unroll
-    for(int o = 0; o < 4; o++)
+    for(int o = 0; o < G::RPT; o++)
     {
       const int k = i - o;
       if(k < 0 || k >= WIN) continue;
@@ -128,30 +161,28 @@ __global__ void __launch_bounds__(kThreads) k_ssim(const SsimJob* __restrict__ j
   const float om = c_om[wi];
   const float cf = (float)c;
   const float k_cc = (float)(c_omd[wi] * (double)c * (double)c * c_w0d[wi]);
-  const float cw0 = cf * w0;
+  const float cw0 = cf * w0, om2c = om * 2.0f * cf, omc = om * cf;
   const float C1 = J.c1, C2 = J.c2;
-  float rows[4];
+  const bool calc_l = J.calc_l != 0;
   #pragma unroll
-  for(int o = 0; o < 4; o++)
+  for(int o = 0; o < G::RPT; o++)
   {
     const float S1a = acc[o][0], S1b = acc[o][1], S2a = acc[o][2], S2b = acc[o][3], Sab = acc[o][4];
-    const float mua = S1a + cw0, mub = S1b + cw0;
-    const float va = S2a - S1a * S1a + fmaf(om * 2.0f * cf, S1a, k_cc);
-    const float vb = S2b - S1b * S1b + fmaf(om * 2.0f * cf, S1b, k_cc);
-    const float cov = Sab - S1a * S1b + fmaf(om * cf, S1a + S1b, k_cc);
-    float v = __fdiv_rn(2.0f * cov + C2, va + vb + C2);
-    if(J.calc_l) v *= __fdiv_rn(2.0f * mua * mub + C1, mua * mua + mub * mub + C1);
-    const int y = y0 + rg * 4 + o, x = x0 + col;
-    rows[o] = (y < y1 && x < x1) ? v : 0.0f;
-  }
-  #pragma unroll
-  for(int o = 0; o < 4; o++)
-  {
-    float s = rows[o];
+    const float va = S2a - S1a * S1a + fmaf(om2c, S1a, k_cc);
+    const float vb = S2b - S1b * S1b + fmaf(om2c, S1b, k_cc);
+    const float cov = Sab - S1a * S1b + fmaf(omc, S1a + S1b, k_cc);
+    float num = 2.0f * cov + C2, den = va + vb + C2;
+    if(calc_l)
+    { // L * CS = (nL nCS) / (dL dCS): one division (xStructSim.cpp:50-51)
+      const float mua = S1a + cw0, mub = S1b + cw0;
+      num *= 2.0f * mua * mub + C1;
+      den *= mua * mua + mub * mub + C1;
+    }
+    const int y = y0 + warp * G::RPT + o, x = x0 + lane;
+    float v = (y < y1 && x < x1) ? __fdividef(num, den) : 0.0f;
     #pragma unroll
-    for(int d = 16; d > 0; d >>= 1) s += __shfl_xor_sync(0xffffffffu, s, d);
-    const int y = y0 + rg * 4 + o;
-    if(col == 0 && y < y1) J.partial[(int64_t)(y - 5) * J.tiles_x + tx] = s;
+    for(int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
+    if(lane == 0 && y < y1) J.partial[(int64_t)(y - 5) * J.tiles_x + tx] = v;
   }
 }
 
@@ -243,7 +274,11 @@ cudaError_t ssim_set_window_constants(const float g[11], const double w0[2])
 }
 
 int ssim_tiles_x(int W) { return W > 10 ? (W - 10 + kTX - 1) / kTX : 0; }
-int ssim_tiles_y(int H) { return H > 10 ? (H - 10 + kTY - 1) / kTY : 0; }
+int ssim_tiles_y(int H, int window)
+{
+  const int ty = window == QMIV_SSIM_GAUSS11 ? SGeo<11>::TY : SGeo<10>::TY;
+  return H > 10 ? (H - 10 + ty - 1) / ty : 0;
+}
 
 cudaError_t launch_ssim(const SsimJob* d_jobs, const SsimJob* h_jobs, int n, int window, cudaStream_t st)
 {
@@ -251,8 +286,16 @@ cudaError_t launch_ssim(const SsimJob* d_jobs, const SsimJob* h_jobs, int n, int
   for(int i = 0; i < n; i++) blocks = h_jobs[i].tile_base + h_jobs[i].tiles_x * h_jobs[i].tiles_y;
   if(blocks > 0)
   {
-    if(window == QMIV_SSIM_GAUSS11) k_ssim<11><<<blocks, kThreads, 0, st>>>(d_jobs, n);
-    else                            k_ssim<10><<<blocks, kThreads, 0, st>>>(d_jobs, n);
+    static bool attr = false;
+    if(!attr)
+    {
+      cudaError_t e = cudaFuncSetAttribute(k_ssim<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, SGeo<10>::SMEM);
+      if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim<11>, cudaFuncAttributeMaxDynamicSharedMemorySize, SGeo<11>::SMEM);
+      if(e != cudaSuccess) return e;
+      attr = true;
+    }
+    if(window == QMIV_SSIM_GAUSS11) k_ssim<11><<<blocks, kThreads, SGeo<11>::SMEM, st>>>(d_jobs, n);
+    else                            k_ssim<10><<<blocks, kThreads, SGeo<10>::SMEM, st>>>(d_jobs, n);
     cudaError_t e = cudaGetLastError();
     if(e != cudaSuccess) return e;
   }

@@ -459,7 +459,7 @@ void add_ssim_job(qmiv_handle* h, const SsimPlane& a, const SsimPlane& b, int W,
   s.c1 = (float)((0.01 * mx) * (0.01 * mx)); // xSSIM.cpp:21-23
   s.c2 = (float)((0.03 * mx) * (0.03 * mx));
   s.tiles_x = ssim_tiles_x(W);
-  s.tiles_y = ssim_tiles_y(H);
+  s.tiles_y = ssim_tiles_y(H, h->opt.ssim_window);
   s.partial = partial;
   s.out = out;
   partial += (size_t)std::max(0, H - 10) * s.tiles_x;
