@@ -6,14 +6,17 @@
 // The reference evaluates 10x10 (REF10) window moments in FP64 with FP32 coefficients per
 // output pixel (800 multiply-adds). Here the window is separable: the coefficient table is
 // the outer product of the normalised 11-tap Gaussian g rounded to 10 decimals, so the
-// moments are computed as a horizontal then a vertical 10-tap (or 11-tap) pass in FP32
-// (~100 multiply-adds per pixel), on samples centred by a per-tile integer offset c so that
+// moments are computed as a vertical then a horizontal 10-tap (or 11-tap) pass in FP32
+// (~80 multiply-adds per pixel), on samples centred by a per-tile integer offset c so that
 // E[x^2] - E[x]^2 does not cancel. With W0 = (sum g)^2 the moments about zero follow from
 // the centred sums S1 = sum w (x-c), S2 = sum w (x-c)^2:
 //   mu  = S1 + c W0,   var = S2 - S1^2 + (1-W0)(2c S1 + c^2 W0),
 //   cov = Sxy - S1x S1y + (1-W0)(c (S1x + S1y) + c^2 W0).
-// Rows are summed per 32-pixel tile in FP32 and across tiles and rows in FP64 (compensated),
-// the picture sum divided by W*H as the reference does.
+// Only var_a + var_b enters the index, so four moment streams are filtered per pixel:
+// S1a, S1b, S(a^2 + b^2) and S(ab). Two vertically adjacent rows travel together in one
+// float2 through Blackwell's packed FP32 multiply-add (FFMA2), which halves the issue slots
+// of the filter taps. Rows are summed per tile in FP32 and across tiles and rows in FP64
+// (compensated), the picture sum divided by W*H as the reference does.
 #include <cfloat>
 
 #include "qmiv_device.cuh"
@@ -22,6 +25,7 @@
 namespace qmiv {
 
 __constant__ float c_g[11];      // 1-D window factor
+__constant__ float2 c_g2[11];    // (g, g) pairs for the packed filter
 __constant__ float c_w0[2];      // W0 = (sum g)^2 for the 10- and 11-tap windows
 __constant__ float c_om[2];      // 1 - W0, rounded from FP64 (not formed in FP32)
 __constant__ double c_w0d[2];
@@ -29,14 +33,18 @@ __constant__ double c_omd[2];
 
 namespace {
 
-constexpr int kTX = 32, kThreads = 256, kIH = 64;  // staged rows: output rows + window - 1
+// Tile geometry. A block of 256 threads stages a 64-column strip of IH rows of both planes,
+// filters it vertically into TY output rows (thread = staged column x 8 output rows, rows
+// paired in float2), then horizontally (thread = output row pair x 4 output columns).
+constexpr int kThreads = 256, kIW = 64, kTY = 32, kPairs = kTY / 2, kGroups = 14, kPS = 67;
 template <int WIN> struct SGeo {
-  static constexpr int TY = kIH - WIN + 1;          // 55 output rows (REF10), 54 (GAUSS11)
-  static constexpr int IW = kTX + WIN - 1;          // staged columns
-  static constexpr int RS = ((IW + 2) / 4) * 4 + 1; // row stride = 1 (mod 4): conflict-free h-pass reads
-  static constexpr int HS = kTX + 1;                // h-moment row stride (= 1 mod 4)
-  static constexpr int RPT = (TY + 7) / 8;          // output rows per thread in the v-pass
-  static constexpr int SMEM = (2 * kIH * RS + 5 * kIH * HS) * 4;
+  static constexpr int TX = kIW - WIN + 1;          // 55 output columns (REF10), 54 (GAUSS11)
+  static constexpr int IH = kTY + WIN - 1;          // staged rows
+  static constexpr int RPW = (IH + 7) / 8;          // staged rows per warp
+  // staged planes [2][IH][64] floats, vertical moments [4][16 pairs][kPS] float2 (odd pitch:
+  // conflict-free reads down a column), row-pair reduction [7][16] float2
+  static constexpr int SMEM = 2 * IH * kIW * 4 + 4 * kPairs * kPS * 8 + 7 * kPairs * 8;
+  static_assert(4 * kGroups >= TX && 4 * (kGroups - 1) + 3 + WIN - 1 < kPS, "tile columns");
 };
 
 __device__ __forceinline__ int ld_plane(const SsimPlane& p, int x, int y)
@@ -52,137 +60,177 @@ __device__ __forceinline__ int find_ssim_job(const SsimJob* __restrict__ jobs, i
   return lo;
 }
 
-// Stage one plane's rows (warp per row, lanes along x) as centred floats; rows and columns past
-// the picture clamp (they only feed outputs outside the valid region).
-template <typename T, int SH, int IW, int RS>
+// Stage one plane: warp w loads rows w, w+8, ..., lanes the columns lane and lane+32; all loads
+// are issued before the first store. Rows and columns past the picture clamp (they only feed
+// outputs outside the valid region).
+template <typename T, int SH, int IH>
 __device__ __forceinline__ void stage_rows(const SsimPlane& P, float* dst, int x0, int y0, int W, int H, int c)
 {
+  constexpr int RPW = (IH + 7) / 8;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for(int r = warp; r < kIH; r += kThreads / 32)
+  const T* base = reinterpret_cast<const T*>(P.ptr);
+  const int gx0 = min(x0 - 5 + lane, W - 1) >> SH, gx1 = min(x0 + 27 + lane, W - 1) >> SH;
+  int v[RPW][2];
+  #pragma unroll
+  for(int k = 0; k < RPW; k++)
   {
-    const int gy = min(y0 - 5 + r, H - 1);
-    const T* row = reinterpret_cast<const T*>(P.ptr) + (int64_t)(gy >> SH) * P.stride;
-    for(int q = lane; q < IW; q += 32)
+    const int i = min(warp + 8 * k, IH - 1);
+    const T* row = base + (int64_t)(min(y0 - 5 + i, H - 1) >> SH) * P.stride;
+    v[k][0] = __ldg(row + gx0);
+    v[k][1] = __ldg(row + gx1);
+  }
+  #pragma unroll
+  for(int k = 0; k < RPW; k++)
+  {
+    const int i = warp + 8 * k;
+    if(i < IH)
     {
-      const int gx = min(x0 - 5 + q, W - 1);
-      dst[r * RS + q] = (float)((int)__ldg(row + (gx >> SH)) - c);
+      dst[i * kIW + lane] = (float)(v[k][0] - c);
+      dst[i * kIW + lane + 32] = (float)(v[k][1] - c);
     }
   }
 }
 
-template <int IW, int RS>
+template <int IH>
 __device__ __forceinline__ void stage_plane(const SsimPlane& P, float* dst, int x0, int y0, int W, int H, int c)
 {
-  if(P.sbytes == 1) { if(P.shift) stage_rows<uint8_t, 1, IW, RS>(P, dst, x0, y0, W, H, c); else stage_rows<uint8_t, 0, IW, RS>(P, dst, x0, y0, W, H, c); }
-  else              { if(P.shift) stage_rows<uint16_t, 1, IW, RS>(P, dst, x0, y0, W, H, c); else stage_rows<uint16_t, 0, IW, RS>(P, dst, x0, y0, W, H, c); }
+  if(P.sbytes == 1) { if(P.shift) stage_rows<uint8_t, 1, IH>(P, dst, x0, y0, W, H, c); else stage_rows<uint8_t, 0, IH>(P, dst, x0, y0, W, H, c); }
+  else              { if(P.shift) stage_rows<uint16_t, 1, IH>(P, dst, x0, y0, W, H, c); else stage_rows<uint16_t, 0, IH>(P, dst, x0, y0, W, H, c); }
 }
 
+__device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
+
 template <int WIN>
-__global__ void __launch_bounds__(kThreads) k_ssim(const SsimJob* __restrict__ jobs, int njobs)
+__global__ void __launch_bounds__(kThreads, 3) k_ssim(const SsimJob* __restrict__ jobs, int njobs)
 {
   using G = SGeo<WIN>;
-  extern __shared__ float smem[];
-  float* s_in = smem;                       // [2][kIH][RS]
-  float* s_h = smem + 2 * kIH * G::RS;      // [5][kIH][HS]
-  __shared__ int s_c;
+  extern __shared__ __align__(16) float smem[];
+  float* s_in = smem;                                              // [2][IH][64]
+  float2* s_v = reinterpret_cast<float2*>(smem + 2 * G::IH * kIW); // [4][16][kPS]
+  float2* s_red = s_v + 4 * kPairs * kPS;                          // [7][16]
 
   const int jb = find_ssim_job(jobs, njobs, blockIdx.x);
   const SsimJob& J = jobs[jb];
   const int local = blockIdx.x - J.tile_base;
   const int ty = local / J.tiles_x, tx = local - ty * J.tiles_x;
   const int W = J.W, H = J.H;
-  const int x0 = 5 + tx * kTX, y0 = 5 + ty * G::TY;
-  const int x1 = min(x0 + kTX, W - 5), y1 = min(y0 + G::TY, H - 5);
+  const int x0 = 5 + tx * G::TX, y0 = 5 + ty * kTY;
+  const int x1 = min(x0 + G::TX, W - 5), y1 = min(y0 + kTY, H - 5);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
-  if(tid == 0) s_c = ld_plane(J.b, min((x0 + x1) >> 1, W - 1), min((y0 + y1) >> 1, H - 1));
-  __syncthreads();
-  const int c = s_c;
-  stage_plane<G::IW, G::RS>(J.a, s_in, x0, y0, W, H, c);
-  stage_plane<G::IW, G::RS>(J.b, s_in + kIH * G::RS, x0, y0, W, H, c);
+  // centring offset: the tile-centre sample of plane b (every thread loads the same address)
+  const int c = ld_plane(J.b, min((x0 + x1) >> 1, W - 1), min((y0 + y1) >> 1, H - 1));
+  stage_plane<G::IH>(J.a, s_in, x0, y0, W, H, c);
+  stage_plane<G::IH>(J.b, s_in + G::IH * kIW, x0, y0, W, H, c);
   __syncthreads();
 
-  // horizontal pass: item = (row, 4 consecutive output columns); 8 items per row
-  #pragma unroll 1
-  for(int item = tid; item < kIH * (kTX / 4); item += kThreads)
+  // vertical pass: column q, output rows 8rg .. 8rg+7 as four row pairs; position i holds
+  // the staged rows (8rg+i, 8rg+i+1), which output pair u takes with weight g[i - 2u]
   {
-    const int r = item >> 3, q0 = (item & 7) * 4;
-    float a[4 + WIN - 1], b[4 + WIN - 1], aa[4 + WIN - 1], bb[4 + WIN - 1], ab[4 + WIN - 1];
+    const int q = tid & (kIW - 1), rg = tid >> 6;
+    const float* sa = s_in + 8 * rg * kIW + q;
+    const float* sb = sa + G::IH * kIW;
+    float2 acc[4][4];
     #pragma unroll
-    for(int i = 0; i < 4 + WIN - 1; i++)
-    {
-      a[i] = s_in[r * G::RS + q0 + i];
-      b[i] = s_in[kIH * G::RS + r * G::RS + q0 + i];
-      aa[i] = a[i] * a[i]; bb[i] = b[i] * b[i]; ab[i] = a[i] * b[i];
-    }
-    #pragma unroll
-    for(int o = 0; o < 4; o++)
-    {
-      float m0 = 0.f, m1 = 0.f, m2 = 0.f, m3 = 0.f, m4 = 0.f;
+    for(int u = 0; u < 4; u++)
       #pragma unroll
-      for(int k = 0; k < WIN; k++)
+      for(int s = 0; s < 4; s++) acc[u][s] = make_float2(0.f, 0.f);
+    #pragma unroll
+    for(int i = 0; i < 6 + WIN; i++)
+    {
+      const float2 pa = make_float2(sa[i * kIW], sa[(i + 1) * kIW]);
+      const float2 pb = make_float2(sb[i * kIW], sb[(i + 1) * kIW]);
+      const float2 pq = __ffma2_rn(pa, pa, __fmul2_rn(pb, pb));
+      const float2 px = __fmul2_rn(pa, pb);
+      #pragma unroll
+      for(int u = 0; u < 4; u++)
       {
-        const float g = c_g[k];
-        m0 = fmaf(g, a[o + k], m0); m1 = fmaf(g, b[o + k], m1);
-        m2 = fmaf(g, aa[o + k], m2); m3 = fmaf(g, bb[o + k], m3); m4 = fmaf(g, ab[o + k], m4);
+        const int k = i - 2 * u;
+        if(k < 0 || k >= WIN) continue;
+        const float2 g = c_g2[k];
+        acc[u][0] = __ffma2_rn(g, pa, acc[u][0]);
+        acc[u][1] = __ffma2_rn(g, pb, acc[u][1]);
+        acc[u][2] = __ffma2_rn(g, pq, acc[u][2]);
+        acc[u][3] = __ffma2_rn(g, px, acc[u][3]);
       }
-      float* h = s_h + r * G::HS + q0 + o;
-      h[0] = m0; h[kIH * G::HS] = m1; h[2 * kIH * G::HS] = m2; h[3 * kIH * G::HS] = m3; h[4 * kIH * G::HS] = m4;
     }
+    #pragma unroll
+    for(int u = 0; u < 4; u++)
+      #pragma unroll
+      for(int s = 0; s < 4; s++) s_v[(s * kPairs + 4 * rg + u) * kPS + q] = acc[u][s];
   }
   __syncthreads();
 
-  // vertical pass: lane = column, warp = RPT consecutive output rows
-  float acc[G::RPT][5];
-  #pragma unroll
-  for(int o = 0; o < G::RPT; o++)
-    #pragma unroll
-    for(int m = 0; m < 5; m++) acc[o][m] = 0.f;
-  #pragma unroll
-  for(int i = 0; i < G::RPT + WIN - 1; i++)
+  // horizontal pass and the index: row pair p (lanes 0-15 / 16-31), output columns 4gi .. 4gi+3
+  if(warp < 7)
   {
-    const int r = min(warp * G::RPT + i, kIH - 1);
-    float hv[5];
+    const int p = lane & 15, gi = 2 * warp + (lane >> 4), j0 = 4 * gi;
+    float2 m[4][4];                                                 // [column][stream]
     #pragma unroll
-    for(int m = 0; m < 5; m++) hv[m] = s_h[m * kIH * G::HS + r * G::HS + lane];
-    #pragma unroll
-    for(int o = 0; o < G::RPT; o++)
+    for(int s = 0; s < 4; s++)
     {
-      const int k = i - o;
-      if(k < 0 || k >= WIN) continue;
-      const float g = c_g[k];
+      const float2* v = s_v + (s * kPairs + p) * kPS + j0;
       #pragma unroll
-      for(int m = 0; m < 5; m++) acc[o][m] = fmaf(g, hv[m], acc[o][m]);
+      for(int jj = 0; jj < 4; jj++) m[jj][s] = make_float2(0.f, 0.f);
+      #pragma unroll
+      for(int t = 0; t < 3 + WIN; t++)
+      {
+        const float2 val = v[t];
+        #pragma unroll
+        for(int jj = 0; jj < 4; jj++)
+        {
+          const int k = t - jj;
+          if(k < 0 || k >= WIN) continue;
+          m[jj][s] = __ffma2_rn(c_g2[k], val, m[jj][s]);
+        }
+      }
     }
-  }
 
-  const int wi = WIN == 11 ? 1 : 0;
-  const float w0 = c_w0[wi];
-  const float om = c_om[wi];
-  const float cf = (float)c;
-  const float k_cc = (float)(c_omd[wi] * (double)c * (double)c * c_w0d[wi]);
-  const float cw0 = cf * w0, om2c = om * 2.0f * cf, omc = om * cf;
-  const float C1 = J.c1, C2 = J.c2;
-  const bool calc_l = J.calc_l != 0;
-  #pragma unroll
-  for(int o = 0; o < G::RPT; o++)
-  {
-    const float S1a = acc[o][0], S1b = acc[o][1], S2a = acc[o][2], S2b = acc[o][3], Sab = acc[o][4];
-    const float va = S2a - S1a * S1a + fmaf(om2c, S1a, k_cc);
-    const float vb = S2b - S1b * S1b + fmaf(om2c, S1b, k_cc);
-    const float cov = Sab - S1a * S1b + fmaf(omc, S1a + S1b, k_cc);
-    float num = 2.0f * cov + C2, den = va + vb + C2;
-    if(calc_l)
-    { // L * CS = (nL nCS) / (dL dCS): one division (xStructSim.cpp:50-51)
-      const float mua = S1a + cw0, mub = S1b + cw0;
-      num *= 2.0f * mua * mub + C1;
-      den *= mua * mua + mub * mub + C1;
-    }
-    const int y = y0 + warp * G::RPT + o, x = x0 + lane;
-    float v = (y < y1 && x < x1) ? __fdividef(num, den) : 0.0f;
+    const int wi = WIN == 11 ? 1 : 0;
+    const float cf = (float)c;
+    const float k_cc = (float)(c_omd[wi] * (double)c * (double)c * c_w0d[wi]);
+    const float2 cw0 = f2(cf * c_w0[wi]), om2c = f2(c_om[wi] * 2.0f * cf), omc = f2(c_om[wi] * cf);
+    const float2 vq0 = f2(2.0f * k_cc + J.c2), cv0 = f2(k_cc), two = f2(2.0f), c1 = f2(J.c1), c2 = f2(J.c2);
+    const bool calc_l = J.calc_l != 0;
+    const int ya = y0 + 2 * p;
+    const bool row0 = ya < y1, row1 = ya + 1 < y1;
+    float2 rs = make_float2(0.f, 0.f);
     #pragma unroll
-    for(int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
-    if(lane == 0 && y < y1) J.partial[(int64_t)(y - 5) * J.tiles_x + tx] = v;
+    for(int jj = 0; jj < 4; jj++)
+    {
+      const float2 S1a = m[jj][0], S1b = m[jj][1], Sq = m[jj][2], Sx = m[jj][3];
+      const float2 sab = __fadd2_rn(S1a, S1b);
+      const float2 na = make_float2(-S1a.x, -S1a.y);
+      // den: var_a + var_b + C2; num: 2 cov + C2
+      float2 den = __ffma2_rn(om2c, sab, vq0);
+      den = __fadd2_rn(den, __ffma2_rn(na, S1a, Sq));
+      den = __ffma2_rn(make_float2(-S1b.x, -S1b.y), S1b, den);
+      float2 cov = __ffma2_rn(omc, sab, cv0);
+      cov = __fadd2_rn(cov, __ffma2_rn(na, S1b, Sx));
+      float2 num = __ffma2_rn(two, cov, c2);
+      if(calc_l)
+      { // L * CS = (nL nCS) / (dL dCS): one division (xStructSim.cpp:50-51)
+        const float2 mua = __fadd2_rn(S1a, cw0), mub = __fadd2_rn(S1b, cw0);
+        num = __fmul2_rn(num, __ffma2_rn(__fmul2_rn(two, mua), mub, c1));
+        den = __fmul2_rn(den, __ffma2_rn(mua, mua, __ffma2_rn(mub, mub, c1)));
+      }
+      const bool col = x0 + j0 + jj < x1;
+      rs.x += (col && row0) ? __fdividef(num.x, den.x) : 0.0f;
+      rs.y += (col && row1) ? __fdividef(num.y, den.y) : 0.0f;
+    }
+    rs.x += __shfl_xor_sync(0xffffffffu, rs.x, 16);
+    rs.y += __shfl_xor_sync(0xffffffffu, rs.y, 16);
+    if(lane < 16) s_red[warp * kPairs + p] = rs;
+  }
+  __syncthreads();
+  if(tid < kTY)
+  { // row tid of the tile: fixed-order sum over the 7 column warps
+    const float* red = reinterpret_cast<const float*>(s_red) + ((tid >> 1) << 1) + (tid & 1);
+    float s = 0.0f;
+    #pragma unroll
+    for(int w = 0; w < 7; w++) s += red[w * 2 * kPairs];
+    const int y = y0 + tid;
+    if(y < y1) J.partial[(int64_t)(y - 5) * J.tiles_x + tx] = s;
   }
 }
 
@@ -265,7 +313,10 @@ cudaError_t ssim_set_window_constants(const float g[11], const double w0[2])
   const float w0f[2] = { (float)w0[0], (float)w0[1] };
   const double omd[2] = { 1.0 - w0[0], 1.0 - w0[1] };
   const float omf[2] = { (float)omd[0], (float)omd[1] };
+  float2 g2[11];
+  for(int k = 0; k < 11; k++) g2[k] = make_float2(g[k], g[k]);
   cudaError_t e = cudaMemcpyToSymbol(c_g, g, sizeof(float) * 11);
+  if(e == cudaSuccess) e = cudaMemcpyToSymbol(c_g2, g2, sizeof(g2));
   if(e == cudaSuccess) e = cudaMemcpyToSymbol(c_w0, w0f, sizeof(w0f));
   if(e == cudaSuccess) e = cudaMemcpyToSymbol(c_om, omf, sizeof(omf));
   if(e == cudaSuccess) e = cudaMemcpyToSymbol(c_w0d, w0, sizeof(double) * 2);
@@ -273,12 +324,12 @@ cudaError_t ssim_set_window_constants(const float g[11], const double w0[2])
   return e;
 }
 
-int ssim_tiles_x(int W) { return W > 10 ? (W - 10 + kTX - 1) / kTX : 0; }
-int ssim_tiles_y(int H, int window)
+int ssim_tiles_x(int W, int window)
 {
-  const int ty = window == QMIV_SSIM_GAUSS11 ? SGeo<11>::TY : SGeo<10>::TY;
-  return H > 10 ? (H - 10 + ty - 1) / ty : 0;
+  const int tx = window == QMIV_SSIM_GAUSS11 ? SGeo<11>::TX : SGeo<10>::TX;
+  return W > 10 ? (W - 10 + tx - 1) / tx : 0;
 }
+int ssim_tiles_y(int H) { return H > 10 ? (H - 10 + kTY - 1) / kTY : 0; }
 
 cudaError_t launch_ssim(const SsimJob* d_jobs, const SsimJob* h_jobs, int n, int window, cudaStream_t st)
 {

@@ -458,8 +458,8 @@ void add_ssim_job(qmiv_handle* h, const SsimPlane& a, const SsimPlane& b, int W,
   const double mx = (double)((1 << bd) - 1);
   s.c1 = (float)((0.01 * mx) * (0.01 * mx)); // xSSIM.cpp:21-23
   s.c2 = (float)((0.03 * mx) * (0.03 * mx));
-  s.tiles_x = ssim_tiles_x(W);
-  s.tiles_y = ssim_tiles_y(H, h->opt.ssim_window);
+  s.tiles_x = ssim_tiles_x(W, h->opt.ssim_window);
+  s.tiles_y = ssim_tiles_y(H);
   s.partial = partial;
   s.out = out;
   partial += (size_t)std::max(0, H - 10) * s.tiles_x;
@@ -775,9 +775,10 @@ qmiv_status qmiv_create(qmiv_handle** out, const qmiv_options* opt, int32_t max_
   pyr_b = align256(pyr_b);
   if(sm & kSsimMetrics)
   {
-    const size_t full = (size_t)max_h * ssim_tiles_x(max_w);
+    // sized for the 11-tap window, whose narrower tiles give the most tiles per row
+    const size_t full = (size_t)max_h * ssim_tiles_x(max_w, QMIV_SSIM_GAUSS11);
     part_floats = 12 * full;
-    for(int sc = 1; sc <= 4; sc++) part_floats += 3 * (size_t)(max_h >> sc) * ssim_tiles_x(max_w >> sc);
+    for(int sc = 1; sc <= 4; sc++) part_floats += 3 * (size_t)(max_h >> sc) * ssim_tiles_x(max_w >> sc, QMIV_SSIM_GAUSS11);
   }
   h->slot_partial_floats = part_floats;
   const size_t part_b = align256(part_floats * sizeof(float) + 16);

@@ -48,8 +48,8 @@ struct SsimFrame {
 constexpr int kSsimVals = 24;
 
 cudaError_t ssim_set_window_constants(const float g[11], const double w0[2]);
-int ssim_tiles_x(int W);
-int ssim_tiles_y(int H, int window);
+int ssim_tiles_x(int W, int window);
+int ssim_tiles_y(int H);
 cudaError_t launch_ssim(const SsimJob* d_jobs, const SsimJob* h_jobs, int n, int window, cudaStream_t st);
 cudaError_t launch_downsample(const PyrStep* d_steps, const PyrStep* h_steps, int n, cudaStream_t st);
 cudaError_t launch_ssim_combine(const SsimFrame* d_frames, int n, const Params& p, cudaStream_t st);
