@@ -161,6 +161,21 @@ qmiv_status qmiv_gcd(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1,
 /* xPSNR::calcPicPSNR (xPSNR.cpp:17) and xWSPSNR::calcPicWSPSNR (xWSPSNR.cpp:17) */
 qmiv_status qmiv_psnr(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, double psnr[4],
                       double wspsnr[4], qmiv_stream stream);
+/* PSNR and GCD_R2T of one pair of device pictures with no handle and no allocation. No
+ * counterpart in the reference: it exists for callers that cannot allocate device memory
+ * when they measure, such as code running inside an allocator or memory-pool callback,
+ * where an allocation could re-enter the allocator, or a process whose device memory is
+ * all handed to one caching allocator up front, and that have nowhere to keep a handle.
+ * It runs a variant of the statistics kernel whose scratch (per-row sums, the block counter
+ * and the result) is one static device array of about 385 KiB; pictures taller than 8192
+ * rows are rejected with QMIV_TOO_LARGE, host pictures with QMIV_BAD_ARG. opt may be null
+ * (defaults); it supplies unnoticeable, cmp_w_avg and fake_exact. Fills out->psnr,
+ * psnr_pic, gcd_r2t and exact; every other field is 0. Synchronous on `stream`.
+ * The first call on each device looks up the static array's address and should be made
+ * before any stream capture begins. All callers on a device share the one array: calls that
+ * overlap in time, from other threads or on other streams, race and must be serialised. */
+qmiv_status qmiv_psnr_static(const qmiv_pic* pic0, const qmiv_pic* pic1, const qmiv_options* opt,
+                             qmiv_frame_result* out, qmiv_stream stream);
 /* xIVPSNR::calcPicIVPSNR(Tst=P0, Ref=P1, GCD) (xIVPSNR.cpp:32-56); gcd_r2t may be null (computed) */
 qmiv_status qmiv_ivpsnr(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, const int32_t* gcd_r2t,
                         double* ivpsnr, double* r2t, double* t2r, qmiv_stream stream);

@@ -10,6 +10,8 @@
 // 4:2:0). For 4:2:0 the chroma sums of the 4:4:4 picture the reference works on are exact
 // multiples of the native chroma sums (each chroma sample is replicated 2x2,
 // xPixelOpsSTD.cpp:30-49), so the upsampled planes are never formed.
+#include <mutex>
+
 #include "qmiv_device.cuh"
 
 namespace qmiv {
@@ -233,6 +235,104 @@ cudaError_t launch_stats(const DevJob* d_jobs, const DevJob* h_jobs, int n, cons
   for(int i = 0; i < n; i++) blocks = h_jobs[i].stat_base + h_jobs[i].stat_blocks;
   if(blocks == 0) return cudaSuccess;
   k_stats<<<blocks, kStatsThreads, 0, st>>>(d_jobs, n, p);
+  return cudaGetLastError();
+}
+
+// ---- statistics without any allocation --------------------------------------------------
+// The same per-row statistics and last-block finalisation for one picture pair, with the job
+// passed by value (no device job table) and the per-row sums, the counters and the result in
+// one static device array instead of a handle's scratch. It serves callers that cannot
+// allocate device memory at the point of the call.
+
+namespace {
+
+constexpr size_t kStaticRowsBytes = (size_t)kStaticMaxRows * 6 * sizeof(int64_t);
+constexpr size_t kStaticScalarsOff = kStaticRowsBytes;
+constexpr size_t kStaticResultOff = kStaticScalarsOff + ((sizeof(JobScalars) + 255) & ~(size_t)255);
+constexpr size_t kStaticBytes = kStaticResultOff + ((sizeof(qmiv_frame_result) + 255) & ~(size_t)255);
+
+// ~385 KiB: [kStaticMaxRows][6] row sums, then JobScalars, then the frame result
+static __device__ __align__(256) unsigned char g_stats_scratch[kStaticBytes];
+
+__global__ void __launch_bounds__(kStatsThreads) k_stats_static(const DevJob J, Params p)
+{
+  __shared__ double scratch[2 * (kStatsThreads / 32)];
+  __shared__ bool is_last;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int y = 2 * (blockIdx.x * kRowPairsPerBlock + w);
+
+  if(y < J.H)
+  {
+    int sd[2][3] = { { 0, 0, 0 }, { 0, 0, 0 } };
+    unsigned long long ssd[2][3] = { { 0, 0, 0 }, { 0, 0, 0 } };
+    const bool vec = vec_ok(J);
+    if(J.sbytes == 1) stats_rowpair<uint8_t>(J, y, vec, lane, sd, ssd);
+    else              stats_rowpair<uint16_t>(J, y, vec, lane, sd, ssd);
+    long long v[2][6];
+    #pragma unroll
+    for(int r = 0; r < 2; r++)
+      #pragma unroll
+      for(int c = 0; c < 3; c++)
+      {
+        v[r][c] = (long long)(int)__reduce_add_sync(0xffffffffu, (unsigned)sd[r][c]);
+        v[r][3 + c] = (long long)warp_sum(ssd[r][c]);
+      }
+    if(lane < 12)
+    {
+      const int r = lane / 6, q = lane % 6, c = q % 3;
+      const bool chroma420 = J.cshift && c > 0;
+      long long val = 0;
+      #pragma unroll
+      for(int rr = 0; rr < 2; rr++)
+        #pragma unroll
+        for(int qq = 0; qq < 6; qq++)
+          if(qq == q && rr == (chroma420 ? 0 : r)) val = v[rr][qq];
+      if(y + r < J.H) J.stat_rows[(int64_t)(y + r) * 6 + q] = chroma420 ? 2 * val : val;
+    }
+  }
+
+  __threadfence();
+  __syncthreads();
+  if(threadIdx.x == 0) is_last = atomicAdd(&J.sc->stats_done, 1u) == (unsigned)(J.stat_blocks - 1);
+  __syncthreads();
+  if(is_last)
+  {
+    __threadfence();
+    finalize_stats(J, p, scratch);
+  }
+}
+
+int g_static_ready[kStaticMaxDevices];
+StaticStatsScratch g_static_ptrs[kStaticMaxDevices];
+std::mutex g_static_mu;
+
+}  // namespace
+
+cudaError_t stats_static_scratch(StaticStatsScratch* out)
+{
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if(e != cudaSuccess) return e;
+  if(dev < 0 || dev >= kStaticMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  if(!g_static_ready[dev])
+  { // once per device, with that device current: the address of this module's static array
+    unsigned char* base = nullptr;
+    e = cudaGetSymbolAddress((void**)&base, g_stats_scratch);
+    if(e != cudaSuccess) return e;
+    g_static_ptrs[dev].stat_rows = reinterpret_cast<int64_t*>(base);
+    g_static_ptrs[dev].sc = reinterpret_cast<JobScalars*>(base + kStaticScalarsOff);
+    g_static_ptrs[dev].result = reinterpret_cast<qmiv_frame_result*>(base + kStaticResultOff);
+    g_static_ready[dev] = 1;
+  }
+  *out = g_static_ptrs[dev];
+  return cudaSuccess;
+}
+
+cudaError_t launch_stats_static(const DevJob& j, const Params& p, cudaStream_t st)
+{
+  if(j.stat_blocks == 0) return cudaSuccess;
+  k_stats_static<<<j.stat_blocks, kStatsThreads, 0, st>>>(j, p);
   return cudaGetLastError();
 }
 

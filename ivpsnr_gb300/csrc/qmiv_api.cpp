@@ -956,6 +956,77 @@ qmiv_status qmiv_psnr(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1
   return QMIV_OK;
 }
 
+// PSNR and GCD without a handle: the statistics kernel's static-scratch variant. Nothing is
+// allocated here (no device, pinned or managed memory); the only device memory written is
+// the static array of k_stats.cu and the caller's *out through one copy.
+qmiv_status qmiv_psnr_static(const qmiv_pic* pic0, const qmiv_pic* pic1, const qmiv_options* opt,
+                             qmiv_frame_result* out, qmiv_stream stream)
+{
+  if(!pic0 || !pic1 || !out) return fail(QMIV_BAD_ARG, "pic0, pic1 and out must not be null");
+  qmiv_options o;
+  if(opt) o = *opt; else qmiv_default_options(&o);
+  qmiv_status s = check_options(&o);
+  if(s != QMIV_OK) return s;
+  const qmiv_pic* pics[2] = { pic0, pic1 };
+  for(int i = 0; i < 2; i++)
+  {
+    const qmiv_pic* p = pics[i];
+    if(!p->is_device) return fail(QMIV_BAD_ARG, "pic%d: qmiv_psnr_static takes device pictures only", i);
+    if(p->width < 1 || p->height < 1) return fail(QMIV_BAD_ARG, "pic%d: size %dx%d", i, p->width, p->height);
+    if(p->height > kStaticMaxRows)
+      return fail(QMIV_TOO_LARGE, "pic%d: height %d exceeds the static scratch limit of %d rows", i, p->height, kStaticMaxRows);
+    if(p->bitdepth < 1 || p->bitdepth > 14) return fail(QMIV_BAD_ARG, "pic%d: bit depth %d (1..14)", i, p->bitdepth);
+    if(p->sample_bytes != 1 && p->sample_bytes != 2) return fail(QMIV_BAD_ARG, "pic%d: sample_bytes %d", i, p->sample_bytes);
+    if(p->sample_bytes == 1 && p->bitdepth > 8) return fail(QMIV_BAD_ARG, "pic%d: %d-bit samples in 8-bit storage", i, p->bitdepth);
+    if(p->chroma_format != QMIV_CF420 && p->chroma_format != QMIV_CF444)
+      return fail(QMIV_UNSUPPORTED, "pic%d: chroma format %d", i, p->chroma_format);
+    if(p->chroma_format == QMIV_CF420 && ((p->width | p->height) & 1))
+      return fail(QMIV_UNSUPPORTED, "pic%d: 4:2:0 needs even sizes (%dx%d)", i, p->width, p->height);
+    for(int c = 0; c < 3; c++)
+    {
+      if(!p->plane[c]) return fail(QMIV_BAD_ARG, "pic%d: plane %d is null", i, c);
+      const int w = (c && p->chroma_format == QMIV_CF420) ? p->width / 2 : p->width;
+      if(p->stride[c] < w) return fail(QMIV_BAD_ARG, "pic%d: stride[%d]=%d < width %d", i, c, p->stride[c], w);
+    }
+  }
+  if(pic0->width != pic1->width || pic0->height != pic1->height || pic0->bitdepth != pic1->bitdepth ||
+     pic0->chroma_format != pic1->chroma_format || pic0->sample_bytes != pic1->sample_bytes)
+    return fail(QMIV_BAD_ARG, "pic0 and pic1 differ in size, bit depth, format or sample size");
+
+  StaticStatsScratch ss;
+  CUDA_TRY(stats_static_scratch(&ss));
+  Params p;
+  std::memset(&p, 0, sizeof(p));
+  for(int c = 0; c < 3; c++) p.w_avg[c] = o.cmp_w_avg[c];
+  for(int bd = 0; bd <= 14; bd++)
+    for(int c = 0; c < 3; c++) p.maxdiff_for_bd[bd][c] = rne_f32(o.unnoticeable[c] * (float)((1 << bd) - 1));
+  p.fake_exact = o.fake_exact;
+  DevJob j;
+  std::memset(&j, 0, sizeof(j));
+  for(int c = 0; c < 3; c++)
+  {
+    j.p0[c] = pic0->plane[c]; j.p1[c] = pic1->plane[c];
+    j.stride0[c] = pic0->stride[c]; j.stride1[c] = pic1->stride[c];
+  }
+  j.W = pic0->width; j.H = pic0->height; j.bd = pic0->bitdepth; j.sbytes = pic0->sample_bytes;
+  j.cshift = pic0->chroma_format == QMIV_CF420 ? 1 : 0;
+  j.metrics = QMIV_M_PSNR;
+  j.stat_rows = ss.stat_rows;
+  j.sc = ss.sc;
+  j.result = ss.result;
+  j.stat_blocks = ((j.H + 1) / 2 + 7) / 8;
+  const cudaStream_t st = (cudaStream_t)stream;
+  // the block counter must start at zero; the result is cleared so fields not computed read 0
+  CUDA_TRY(cudaMemsetAsync(ss.sc, 0, sizeof(JobScalars), st));
+  CUDA_TRY(cudaMemsetAsync(ss.result, 0, sizeof(qmiv_frame_result), st));
+  CUDA_TRY(launch_stats_static(j, p, st));
+  CUDA_TRY(cudaMemcpyAsync(out, ss.result, sizeof(qmiv_frame_result), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  out->metrics = QMIV_M_PSNR;
+  if(out->status != 0) return fail(QMIV_CUDA_ERROR, "device status %d", out->status);
+  return QMIV_OK;
+}
+
 qmiv_status qmiv_ivpsnr(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, const int32_t* gcd,
                         double* iv, double* r2t, double* t2r, qmiv_stream stream)
 {

@@ -63,6 +63,18 @@ struct Params {
 // Host-side launchers (defined in the .cu files).
 cudaError_t launch_stats(const DevJob* d_jobs, const DevJob* h_jobs, int n, const Params& p, cudaStream_t st);
 
+// Statistics of one picture pair in a static device array (k_stats.cu): no allocation.
+constexpr int kStaticMaxRows = 8192;     // tallest picture the static row sums hold
+constexpr int kStaticMaxDevices = 64;
+struct StaticStatsScratch {
+  int64_t* stat_rows;                    // [kStaticMaxRows][6]
+  JobScalars* sc;                        // stats_done must be 0 when the kernel starts
+  qmiv_frame_result* result;
+};
+// The array's address on the current device (looked up on the first call per device).
+cudaError_t stats_static_scratch(StaticStatsScratch* out);
+cudaError_t launch_stats_static(const DevJob& j, const Params& p, cudaStream_t st);
+
 // One compiled form of the CPS kernel.
 struct CpsVariant {
   const char* name;
