@@ -13,10 +13,11 @@
 //   mu  = S1 + c W0,   var = S2 - S1^2 + (1-W0)(2c S1 + c^2 W0),
 //   cov = Sxy - S1x S1y + (1-W0)(c (S1x + S1y) + c^2 W0).
 // Only var_a + var_b enters the index, so four moment streams are filtered per pixel:
-// S1a, S1b, S(a^2 + b^2) and S(ab). Two vertically adjacent rows travel together in one
-// float2 through Blackwell's packed FP32 multiply-add (FFMA2), which halves the issue slots
-// of the filter taps. Rows are summed per tile in FP32 and across tiles and rows in FP64
-// (compensated), the picture sum divided by W*H as the reference does.
+// S1a, S1b, S(a^2 + b^2) and S(ab), as two float2 pairs through Blackwell's packed FP32
+// multiply-add (FFMA2), which halves the issue slots of the filter taps. Rows are summed per
+// tile in FP32 and across tiles and rows in FP64 (compensated), the picture sum divided by
+// W*H as the reference does.
+#include <algorithm>
 #include <cfloat>
 
 #include "qmiv_device.cuh"
@@ -33,18 +34,19 @@ __constant__ double c_omd[2];
 
 namespace {
 
-// Tile geometry. A block of 256 threads stages a 64-column strip of IH rows of both planes,
-// filters it vertically into TY output rows (thread = staged column x 8 output rows, rows
-// paired in float2), then horizontally (thread = output row pair x 4 output columns).
-constexpr int kThreads = 256, kIW = 64, kTY = 32, kPairs = kTY / 2, kGroups = 14, kPS = 67;
+// Tile geometry. A persistent block of 256 threads walks the tiles of all jobs; per tile it
+// stages a 64-column strip of IH rows of both planes as (a, b) pairs, filters it vertically
+// into TY output rows (thread = staged column x 8 output rows), then horizontally (thread =
+// output row x 8 output columns) and evaluates the index.
+constexpr int kThreads = 256, kIW = 64, kTY = 32, kRP = 67;
 template <int WIN> struct SGeo {
   static constexpr int TX = kIW - WIN + 1;          // 55 output columns (REF10), 54 (GAUSS11)
   static constexpr int IH = kTY + WIN - 1;          // staged rows
   static constexpr int RPW = (IH + 7) / 8;          // staged rows per warp
-  // staged planes [2][IH][64] floats, vertical moments [4][16 pairs][kPS] float2 (odd pitch:
-  // conflict-free reads down a column), row-pair reduction [7][16] float2
-  static constexpr int SMEM = 2 * IH * kIW * 4 + 4 * kPairs * kPS * 8 + 7 * kPairs * 8;
-  static_assert(4 * kGroups >= TX && 4 * (kGroups - 1) + 3 + WIN - 1 < kPS, "tile columns");
+  // staged (a, b) pairs [IH][64] float2; vertical moments [32][kRP] float4 (S1a, S1b,
+  // S(a^2+b^2), S(ab)) with an odd pitch (conflict-free reads down a column); row sums [7][32]
+  static constexpr int SMEM = IH * kIW * 8 + kTY * kRP * 16 + 7 * kTY * 4;
+  static_assert(8 * 7 >= TX && 8 * 6 + 7 + WIN - 1 < kRP, "tile columns");
 };
 
 __device__ __forceinline__ int ld_plane(const SsimPlane& p, int x, int y)
@@ -53,184 +55,179 @@ __device__ __forceinline__ int ld_plane(const SsimPlane& p, int x, int y)
   return p.sbytes == 1 ? (int)__ldg((const uint8_t*)p.ptr + o) : (int)__ldg((const uint16_t*)p.ptr + o);
 }
 
-__device__ __forceinline__ int find_ssim_job(const SsimJob* __restrict__ jobs, int n, int b)
-{
-  int lo = 0, hi = n - 1;
-  while(lo < hi) { const int mid = (lo + hi + 1) >> 1; if(jobs[mid].tile_base <= b) lo = mid; else hi = mid - 1; }
-  return lo;
-}
-
-// Stage one plane: warp w loads rows w, w+8, ..., lanes the columns lane and lane+32; all loads
-// are issued before the first store. Rows and columns past the picture clamp (they only feed
-// outputs outside the valid region).
+// One plane's part of a staged tile, in registers: warp w takes staged rows w, w+8, ...,
+// lanes the staged columns lane and lane+32. Rows and columns past the picture clamp (they
+// only feed outputs outside the valid region).
 template <typename T, int SH, int IH>
-__device__ __forceinline__ void stage_rows(const SsimPlane& P, float* dst, int x0, int y0, int W, int H, int c)
+__device__ __forceinline__ void load_rows(const SsimPlane& P, int (&v)[(IH + 7) / 8][2], int xs, int ys, int W, int H)
 {
-  constexpr int RPW = (IH + 7) / 8;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const T* base = reinterpret_cast<const T*>(P.ptr);
-  const int gx0 = min(x0 - 5 + lane, W - 1) >> SH, gx1 = min(x0 + 27 + lane, W - 1) >> SH;
-  int v[RPW][2];
+  const int gx0 = min(xs + lane, W - 1) >> SH, gx1 = min(xs + 32 + lane, W - 1) >> SH;
   #pragma unroll
-  for(int k = 0; k < RPW; k++)
+  for(int k = 0; k < (IH + 7) / 8; k++)
   {
     const int i = min(warp + 8 * k, IH - 1);
-    const T* row = base + (int64_t)(min(y0 - 5 + i, H - 1) >> SH) * P.stride;
+    const T* row = base + (int64_t)(min(ys + i, H - 1) >> SH) * P.stride;
     v[k][0] = __ldg(row + gx0);
     v[k][1] = __ldg(row + gx1);
-  }
-  #pragma unroll
-  for(int k = 0; k < RPW; k++)
-  {
-    const int i = warp + 8 * k;
-    if(i < IH)
-    {
-      dst[i * kIW + lane] = (float)(v[k][0] - c);
-      dst[i * kIW + lane + 32] = (float)(v[k][1] - c);
-    }
   }
 }
 
 template <int IH>
-__device__ __forceinline__ void stage_plane(const SsimPlane& P, float* dst, int x0, int y0, int W, int H, int c)
+__device__ __forceinline__ void load_plane(const SsimPlane& P, int (&v)[(IH + 7) / 8][2], int xs, int ys, int W, int H)
 {
-  if(P.sbytes == 1) { if(P.shift) stage_rows<uint8_t, 1, IH>(P, dst, x0, y0, W, H, c); else stage_rows<uint8_t, 0, IH>(P, dst, x0, y0, W, H, c); }
-  else              { if(P.shift) stage_rows<uint16_t, 1, IH>(P, dst, x0, y0, W, H, c); else stage_rows<uint16_t, 0, IH>(P, dst, x0, y0, W, H, c); }
+  if(P.sbytes == 1) { if(P.shift) load_rows<uint8_t, 1, IH>(P, v, xs, ys, W, H); else load_rows<uint8_t, 0, IH>(P, v, xs, ys, W, H); }
+  else              { if(P.shift) load_rows<uint16_t, 1, IH>(P, v, xs, ys, W, H); else load_rows<uint16_t, 0, IH>(P, v, xs, ys, W, H); }
 }
 
-__device__ __forceinline__ float2 f2(float v) { return make_float2(v, v); }
+// Where tile `tile` is: its job (found by a forward scan from jb) and its origin.
+struct TilePos { int jb, tx, x0, y0; };
+template <int TX>
+__device__ __forceinline__ TilePos locate(const SsimJob* __restrict__ jobs, int njobs, int jb, int tile)
+{
+  while(jb + 1 < njobs && jobs[jb + 1].tile_base <= tile) jb++;
+  const int local = tile - jobs[jb].tile_base, tiles_x = jobs[jb].tiles_x;
+  const int ty = local / tiles_x, tx = local - ty * tiles_x;
+  TilePos t; t.jb = jb; t.tx = tx; t.x0 = 5 + tx * TX; t.y0 = 5 + ty * kTY;
+  return t;
+}
+
+__device__ __forceinline__ float2 lo2(const float4& v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(const float4& v) { return make_float2(v.z, v.w); }
 
 template <int WIN>
-__global__ void __launch_bounds__(kThreads, 3) k_ssim(const SsimJob* __restrict__ jobs, int njobs)
+__global__ void __launch_bounds__(kThreads, 3) k_ssim(const SsimJob* __restrict__ jobs, int njobs, int ntiles)
 {
   using G = SGeo<WIN>;
   extern __shared__ __align__(16) float smem[];
-  float* s_in = smem;                                              // [2][IH][64]
-  float2* s_v = reinterpret_cast<float2*>(smem + 2 * G::IH * kIW); // [4][16][kPS]
-  float2* s_red = s_v + 4 * kPairs * kPS;                          // [7][16]
-
-  const int jb = find_ssim_job(jobs, njobs, blockIdx.x);
-  const SsimJob& J = jobs[jb];
-  const int local = blockIdx.x - J.tile_base;
-  const int ty = local / J.tiles_x, tx = local - ty * J.tiles_x;
-  const int W = J.W, H = J.H;
-  const int x0 = 5 + tx * G::TX, y0 = 5 + ty * kTY;
-  const int x1 = min(x0 + G::TX, W - 5), y1 = min(y0 + kTY, H - 5);
+  float2* s_in = reinterpret_cast<float2*>(smem);                    // [IH][64]
+  float4* s_v = reinterpret_cast<float4*>(smem + 2 * G::IH * kIW);   // [32][kRP]
+  float* s_red = smem + 2 * G::IH * kIW + 4 * kTY * kRP;             // [7][32]
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
-  // centring offset: the tile-centre sample of plane b (every thread loads the same address)
-  const int c = ld_plane(J.b, min((x0 + x1) >> 1, W - 1), min((y0 + y1) >> 1, H - 1));
-  stage_plane<G::IH>(J.a, s_in, x0, y0, W, H, c);
-  stage_plane<G::IH>(J.b, s_in + G::IH * kIW, x0, y0, W, H, c);
-  __syncthreads();
-
-  // vertical pass: column q, output rows 8rg .. 8rg+7 as four row pairs; position i holds
-  // the staged rows (8rg+i, 8rg+i+1), which output pair u takes with weight g[i - 2u]
+  // window factor pairs (g, g), kept in registers for the whole kernel
+  float2 gk[WIN];
+  #pragma unroll
+  for(int k = 0; k < WIN; k++)
   {
-    const int q = tid & (kIW - 1), rg = tid >> 6;
-    const float* sa = s_in + 8 * rg * kIW + q;
-    const float* sb = sa + G::IH * kIW;
-    float2 acc[4][4];
+    gk[k] = c_g2[k];
+    asm volatile("" : "+f"(gk[k].x), "+f"(gk[k].y));
+  }
+  const int wi = WIN == 11 ? 1 : 0;
+
+  int jb = 0;
+  for(int tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+  {
+    const TilePos cur = locate<G::TX>(jobs, njobs, jb, tile);
+    jb = cur.jb;
+    const SsimJob& J = jobs[jb];
+    const int tx = cur.tx, x0 = cur.x0, y0 = cur.y0;
+    const int x1 = min(x0 + G::TX, J.W - 5), y1 = min(y0 + kTY, J.H - 5);
+
+    // staging: centring offset c = the tile-centre sample of plane b, loaded with the tile
+    int va[G::RPW][2], vb[G::RPW][2];
+    const int tc = ld_plane(J.b, min((x0 + x1) >> 1, J.W - 1), min((y0 + y1) >> 1, J.H - 1));
+    load_plane<G::IH>(J.a, va, x0 - 5, y0 - 5, J.W, J.H);
+    load_plane<G::IH>(J.b, vb, x0 - 5, y0 - 5, J.W, J.H);
     #pragma unroll
-    for(int u = 0; u < 4; u++)
-      #pragma unroll
-      for(int s = 0; s < 4; s++) acc[u][s] = make_float2(0.f, 0.f);
-    #pragma unroll
-    for(int i = 0; i < 6 + WIN; i++)
+    for(int k = 0; k < G::RPW; k++)
     {
-      const float2 pa = make_float2(sa[i * kIW], sa[(i + 1) * kIW]);
-      const float2 pb = make_float2(sb[i * kIW], sb[(i + 1) * kIW]);
-      const float2 pq = __ffma2_rn(pa, pa, __fmul2_rn(pb, pb));
-      const float2 px = __fmul2_rn(pa, pb);
-      #pragma unroll
-      for(int u = 0; u < 4; u++)
+      const int i = warp + 8 * k;
+      if(i < G::IH)
       {
-        const int k = i - 2 * u;
-        if(k < 0 || k >= WIN) continue;
-        const float2 g = c_g2[k];
-        acc[u][0] = __ffma2_rn(g, pa, acc[u][0]);
-        acc[u][1] = __ffma2_rn(g, pb, acc[u][1]);
-        acc[u][2] = __ffma2_rn(g, pq, acc[u][2]);
-        acc[u][3] = __ffma2_rn(g, px, acc[u][3]);
+        s_in[i * kIW + lane] = make_float2((float)(va[k][0] - tc), (float)(vb[k][0] - tc));
+        s_in[i * kIW + lane + 32] = make_float2((float)(va[k][1] - tc), (float)(vb[k][1] - tc));
       }
     }
-    #pragma unroll
-    for(int u = 0; u < 4; u++)
-      #pragma unroll
-      for(int s = 0; s < 4; s++) s_v[(s * kPairs + 4 * rg + u) * kPS + q] = acc[u][s];
-  }
-  __syncthreads();
+    __syncthreads();
 
-  // horizontal pass and the index: row pair p (lanes 0-15 / 16-31), output columns 4gi .. 4gi+3
-  if(warp < 7)
-  {
-    const int p = lane & 15, gi = 2 * warp + (lane >> 4), j0 = 4 * gi;
-    float2 m[4][4];                                                 // [column][stream]
-    #pragma unroll
-    for(int s = 0; s < 4; s++)
+    // vertical pass: column q, output rows 8rg .. 8rg+7; staged row 8rg+i feeds output row
+    // 8rg+o with weight g[i-o]; (S1a, S1b) and (S(a^2+b^2), S(ab)) travel as float2 pairs
     {
-      const float2* v = s_v + (s * kPairs + p) * kPS + j0;
+      const int q = tid & (kIW - 1), rg = tid >> 6;
+      const float2* src = s_in + 8 * rg * kIW + q;
+      float2 s1[8], sq[8];
       #pragma unroll
-      for(int jj = 0; jj < 4; jj++) m[jj][s] = make_float2(0.f, 0.f);
+      for(int o = 0; o < 8; o++) { s1[o] = make_float2(0.f, 0.f); sq[o] = make_float2(0.f, 0.f); }
       #pragma unroll
-      for(int t = 0; t < 3 + WIN; t++)
+      for(int i = 0; i < 7 + WIN; i++)
       {
-        const float2 val = v[t];
+        const float2 v = src[i * kIW];
+        const float2 p = __fmul2_rn(v, v);
+        const float2 qq = make_float2(p.x + p.y, v.x * v.y);
         #pragma unroll
-        for(int jj = 0; jj < 4; jj++)
+        for(int o = 0; o < 8; o++)
+        {
+          const int k = i - o;
+          if(k < 0 || k >= WIN) continue;
+          s1[o] = __ffma2_rn(gk[k], v, s1[o]);
+          sq[o] = __ffma2_rn(gk[k], qq, sq[o]);
+        }
+      }
+      #pragma unroll
+      for(int o = 0; o < 8; o++) s_v[(8 * rg + o) * kRP + q] = make_float4(s1[o].x, s1[o].y, sq[o].x, sq[o].y);
+    }
+    __syncthreads();
+
+    // horizontal pass and the index: warp w takes output columns 8w .. 8w+7, lane = output row
+    if(warp < 7)
+    {
+      const int o = lane, j0 = 8 * warp;
+      const float4* src = s_v + o * kRP + j0;
+      float2 m1[8], m2[8];
+      #pragma unroll
+      for(int jj = 0; jj < 8; jj++) { m1[jj] = make_float2(0.f, 0.f); m2[jj] = make_float2(0.f, 0.f); }
+      #pragma unroll
+      for(int t = 0; t < 7 + WIN; t++)
+      {
+        const float4 val = src[t];
+        #pragma unroll
+        for(int jj = 0; jj < 8; jj++)
         {
           const int k = t - jj;
           if(k < 0 || k >= WIN) continue;
-          m[jj][s] = __ffma2_rn(c_g2[k], val, m[jj][s]);
+          m1[jj] = __ffma2_rn(gk[k], lo2(val), m1[jj]);
+          m2[jj] = __ffma2_rn(gk[k], hi2(val), m2[jj]);
         }
       }
-    }
-
-    const int wi = WIN == 11 ? 1 : 0;
-    const float cf = (float)c;
-    const float k_cc = (float)(c_omd[wi] * (double)c * (double)c * c_w0d[wi]);
-    const float2 cw0 = f2(cf * c_w0[wi]), om2c = f2(c_om[wi] * 2.0f * cf), omc = f2(c_om[wi] * cf);
-    const float2 vq0 = f2(2.0f * k_cc + J.c2), cv0 = f2(k_cc), two = f2(2.0f), c1 = f2(J.c1), c2 = f2(J.c2);
-    const bool calc_l = J.calc_l != 0;
-    const int ya = y0 + 2 * p;
-    const bool row0 = ya < y1, row1 = ya + 1 < y1;
-    float2 rs = make_float2(0.f, 0.f);
-    #pragma unroll
-    for(int jj = 0; jj < 4; jj++)
-    {
-      const float2 S1a = m[jj][0], S1b = m[jj][1], Sq = m[jj][2], Sx = m[jj][3];
-      const float2 sab = __fadd2_rn(S1a, S1b);
-      const float2 na = make_float2(-S1a.x, -S1a.y);
-      // den: var_a + var_b + C2; num: 2 cov + C2
-      float2 den = __ffma2_rn(om2c, sab, vq0);
-      den = __fadd2_rn(den, __ffma2_rn(na, S1a, Sq));
-      den = __ffma2_rn(make_float2(-S1b.x, -S1b.y), S1b, den);
-      float2 cov = __ffma2_rn(omc, sab, cv0);
-      cov = __fadd2_rn(cov, __ffma2_rn(na, S1b, Sx));
-      float2 num = __ffma2_rn(two, cov, c2);
-      if(calc_l)
-      { // L * CS = (nL nCS) / (dL dCS): one division (xStructSim.cpp:50-51)
-        const float2 mua = __fadd2_rn(S1a, cw0), mub = __fadd2_rn(S1b, cw0);
-        num = __fmul2_rn(num, __ffma2_rn(__fmul2_rn(two, mua), mub, c1));
-        den = __fmul2_rn(den, __ffma2_rn(mua, mua, __ffma2_rn(mub, mub, c1)));
+      const float cf = (float)tc;
+      const float k_cc = (float)(c_omd[wi] * (double)tc * (double)tc * c_w0d[wi]);
+      const float cw0 = cf * c_w0[wi], om2c = c_om[wi] * 2.0f * cf, omc = c_om[wi] * cf;
+      const float vq0 = 2.0f * k_cc + J.c2, cv0 = k_cc, C1 = J.c1, C2 = J.c2;
+      const bool calc_l = J.calc_l != 0;
+      const bool row_ok = y0 + o < y1;
+      float rs = 0.0f;
+      #pragma unroll
+      for(int jj = 0; jj < 8; jj++)
+      {
+        const float S1a = m1[jj].x, S1b = m1[jj].y, Sq = m2[jj].x, Sx = m2[jj].y;
+        const float sab = S1a + S1b;
+        // den: var_a + var_b + C2; num: 2 cov + C2
+        const float den_cs = fmaf(-S1b, S1b, fmaf(-S1a, S1a, Sq)) + fmaf(om2c, sab, vq0);
+        const float cov = fmaf(-S1a, S1b, Sx) + fmaf(omc, sab, cv0);
+        float num = fmaf(2.0f, cov, C2), den = den_cs;
+        if(calc_l)
+        { // L * CS = (nL nCS) / (dL dCS): one division (xStructSim.cpp:50-51)
+          const float mua = S1a + cw0, mub = S1b + cw0;
+          num *= fmaf(2.0f * mua, mub, C1);
+          den *= fmaf(mua, mua, fmaf(mub, mub, C1));
+        }
+        rs += (row_ok && x0 + j0 + jj < x1) ? __fdividef(num, den) : 0.0f;
       }
-      const bool col = x0 + j0 + jj < x1;
-      rs.x += (col && row0) ? __fdividef(num.x, den.x) : 0.0f;
-      rs.y += (col && row1) ? __fdividef(num.y, den.y) : 0.0f;
+      s_red[warp * kTY + o] = rs;
     }
-    rs.x += __shfl_xor_sync(0xffffffffu, rs.x, 16);
-    rs.y += __shfl_xor_sync(0xffffffffu, rs.y, 16);
-    if(lane < 16) s_red[warp * kPairs + p] = rs;
-  }
-  __syncthreads();
-  if(tid < kTY)
-  { // row tid of the tile: fixed-order sum over the 7 column warps
-    const float* red = reinterpret_cast<const float*>(s_red) + ((tid >> 1) << 1) + (tid & 1);
-    float s = 0.0f;
-    #pragma unroll
-    for(int w = 0; w < 7; w++) s += red[w * 2 * kPairs];
-    const int y = y0 + tid;
-    if(y < y1) J.partial[(int64_t)(y - 5) * J.tiles_x + tx] = s;
+    __syncthreads();
+    if(tid < kTY)
+    { // row tid of the tile: fixed-order sum over the 7 column groups
+      float s = 0.0f;
+      #pragma unroll
+      for(int w = 0; w < 7; w++) s += s_red[w * kTY + tid];
+      const int y = y0 + tid;
+      if(y < y1) J.partial[(int64_t)(y - 5) * J.tiles_x + tx] = s;
+    }
+    // the next tile's staging overwrites s_in only; s_v and s_red are rewritten after two
+    // more barriers
   }
 }
 
@@ -333,20 +330,29 @@ int ssim_tiles_y(int H) { return H > 10 ? (H - 10 + kTY - 1) / kTY : 0; }
 
 cudaError_t launch_ssim(const SsimJob* d_jobs, const SsimJob* h_jobs, int n, int window, cudaStream_t st)
 {
-  int blocks = 0;
-  for(int i = 0; i < n; i++) blocks = h_jobs[i].tile_base + h_jobs[i].tiles_x * h_jobs[i].tiles_y;
-  if(blocks > 0)
+  int tiles = 0;
+  for(int i = 0; i < n; i++) tiles = h_jobs[i].tile_base + h_jobs[i].tiles_x * h_jobs[i].tiles_y;
+  if(tiles > 0)
   {
-    static bool attr = false;
-    if(!attr)
+    static int resident[2] = { 0, 0 };  // blocks per SM, per window
+    static int sms = 0;
+    const int wi = window == QMIV_SSIM_GAUSS11 ? 1 : 0;
+    if(!resident[wi])
     {
-      cudaError_t e = cudaFuncSetAttribute(k_ssim<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, SGeo<10>::SMEM);
+      int dev = 0;
+      cudaError_t e = cudaGetDevice(&dev);
+      if(e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, SGeo<10>::SMEM);
       if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim<11>, cudaFuncAttributeMaxDynamicSharedMemorySize, SGeo<11>::SMEM);
+      if(e == cudaSuccess)
+        e = wi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[1], k_ssim<11>, kThreads, SGeo<11>::SMEM)
+               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[0], k_ssim<10>, kThreads, SGeo<10>::SMEM);
       if(e != cudaSuccess) return e;
-      attr = true;
+      if(resident[wi] < 1) resident[wi] = 1;
     }
-    if(window == QMIV_SSIM_GAUSS11) k_ssim<11><<<blocks, kThreads, SGeo<11>::SMEM, st>>>(d_jobs, n);
-    else                            k_ssim<10><<<blocks, kThreads, SGeo<10>::SMEM, st>>>(d_jobs, n);
+    const int grid = std::min(tiles, sms * resident[wi]);
+    if(wi) k_ssim<11><<<grid, kThreads, SGeo<11>::SMEM, st>>>(d_jobs, n, tiles);
+    else   k_ssim<10><<<grid, kThreads, SGeo<10>::SMEM, st>>>(d_jobs, n, tiles);
     cudaError_t e = cudaGetLastError();
     if(e != cudaSuccess) return e;
   }
