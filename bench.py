@@ -37,14 +37,17 @@ WORKLOAD = "multiview-ivpsnr-wspsnr-10bit-420: 3x4096x2048 ERP + 6x1920x1080 + 3
 SMALL = "small-profile-case: 24 pairs 1920x1080 10-bit 4:2:0 (150 MB), SR 2"
 
 
-def jobs_list(small=False):
+def jobs_list(small=False, rank=0, world=1):
+    """This rank's picture pairs (view, frame, w, h, erp). Weak scaling: the job set grows with
+    the number of ranks (frames 0 .. FRAMES*world-1 of every view) and ivpsnr_gb300.shard
+    spreads it by luma area, so every rank gets the 96-pair mix of one GPU."""
+    from ivpsnr_gb300.shard import shard_units
     if small:
-        return [(3, f, 1920, 1080, False) for f in range(24)]
-    out = []
-    for v, (w, h, erp) in enumerate(VIEWS):
-        for f in range(FRAMES):
-            out.append((v, f, w, h, erp))
-    return out
+        units = [(3, f, 1920, 1080, False) for f in range(24 * world)]
+    else:
+        units = [(v, f, w, h, erp) for v, (w, h, erp) in enumerate(VIEWS) for f in range(FRAMES * world)]
+    mine = shard_units([u[2] * u[3] for u in units], rank, world)
+    return [units[i] for i in mine]
 
 
 def dist_env():
@@ -254,7 +257,7 @@ def run_ours(args):
         if rank == 0:
             print(json.dumps(r))
         return
-    jobs = jobs_list(args.workload == "small")
+    jobs = jobs_list(args.workload == "small", rank, world)
     host = make_inputs(jobs)
     devbufs = []
     for (ref, tst) in host:
@@ -313,7 +316,8 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     px_per_step = sum(w * h for (_, _, w, h, _) in jobs)
-    value = px_per_step * world / (ms * 1e-3) / 1e9
+    px_all_ranks = sum(w * h for r in range(world) for (_, _, w, h, _) in jobs_list(args.workload == "small", r, world))
+    value = px_all_ranks / (ms * 1e-3) / 1e9
 
     if args.kernels_only:
         if rank == 0:
@@ -386,7 +390,12 @@ def run_ours(args):
     e1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = e0.elapsed_time(e1) / args.steps
-    e2e_value = px_per_step * world / (e2e_ms * 1e-3) / 1e9
+    barrier()
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = px_all_ranks / (e2e_ms * 1e-3) / 1e9
     P.close()
     Pp.close()
     Pws.close()
