@@ -194,6 +194,36 @@ qmiv_status qmiv_msssim(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pi
 qmiv_status qmiv_ivssim(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, const int32_t* gcd_r2t,
                         double* ivssim, double* r2t, double* t2r, qmiv_stream stream);
 
+/* --- differentiable IV-PSNR error and IV-SSIM ------------------------------------------
+ * No counterpart in the reference (which takes integer samples and has no gradients). Inputs
+ * are n pairs of FP32 4:4:4 pictures with values in [0, 1] (Max = 1), device memory laid out
+ * [n][3][height][width], tst the picture being optimised and ref fixed. The reference's
+ * definitions carry over without integer rounding (opt: search_range 1..4, cmp_w_search,
+ * unnoticeable, ssim_window; null = defaults):
+ *   GCD_c = clip(mean(ref_c - tst_c), +-unnoticeable_c)                          (xGlobClrDiff.cpp:15-48)
+ *   direction 0 (R2T): each tested pixel + GCD searched in ref, first strict minimum of
+ *     sum_c w_c d_c^2 in row-major order, borders clamped; SSE_c = sum of squared errors at the
+ *     argmin (xIVPSNR.cpp:62-95); SSIM_c = SSIM(ref_c, SCP0_c), SCP0 = clip(tst[argmin T2R] + GCD, 0, 1)
+ *   direction 1 (T2R): each ref pixel - GCD searched in tst; SSIM_c = SSIM(tst_c, SCP1_c),
+ *     SCP1 = clip(ref[argmin R2T] - GCD, 0, 1)                                      (xSSIM.cpp:166-190)
+ * so IV-PSNR = min over directions of the weighted 10 log10(W H / SSE_c) and IV-SSIM = min over
+ * directions of the weighted SSIM_c, both formed by the caller from sse[n][2][3] and
+ * ssim[n][2][3] (device FP64). Gradients: the argmin carries none (it is piecewise constant);
+ * errors and SCP samples route to the pixel they were read from; clips pass gradient on their
+ * closed interval; GCD contributes -1/(W H) per pixel while it is not clipped.
+ * The workspace (device, 256-byte aligned, qmiv_loss_workspace_size bytes) is the caller's and
+ * carries the forward state (GCD, argmin maps, SCP planes) to the backward call, which must
+ * see the same inputs and options. g_sse and g_ssim (device FP64, [n][2][3]) are the upstream
+ * gradients; g_tst (device FP32, like tst) receives d loss / d tst. Asynchronous on stream. */
+qmiv_status qmiv_loss_workspace_size(int32_t n, int32_t width, int32_t height, const qmiv_options* opt,
+                                     size_t* bytes);
+qmiv_status qmiv_loss_forward(const float* tst, const float* ref, int32_t n, int32_t width, int32_t height,
+                              const qmiv_options* opt, void* workspace, size_t workspace_bytes, double* sse,
+                              double* ssim, qmiv_stream stream);
+qmiv_status qmiv_loss_backward(const float* tst, const float* ref, int32_t n, int32_t width, int32_t height,
+                               const qmiv_options* opt, void* workspace, size_t workspace_bytes,
+                               const double* g_sse, const double* g_ssim, float* g_tst, qmiv_stream stream);
+
 /* --- per sequence ----------------------------------------------------------------------
  * xMetricStat::calcAvgMetric (xAppQMIV.h:256-260): compensated mean over the frames passed
  * to qmiv_calc_frame since create or the last reset. */

@@ -78,6 +78,10 @@ SIGNATURES = [
     ("qmiv_ssim", c_i32, [_vp, _P(Pic), _P(Pic), c_i32, _P(c_f64), _vp]),
     ("qmiv_msssim", c_i32, [_vp, _P(Pic), _P(Pic), _P(c_f64), _vp]),
     ("qmiv_ivssim", c_i32, [_vp, _P(Pic), _P(Pic), _P(c_i32), _P(c_f64), _P(c_f64), _P(c_f64), _vp]),
+    ("qmiv_loss_workspace_size", c_i32, [c_i32, c_i32, c_i32, _P(Options), _P(ctypes.c_size_t)]),
+    ("qmiv_loss_forward", c_i32, [_vp, _vp, c_i32, c_i32, c_i32, _P(Options), _vp, ctypes.c_size_t, _vp, _vp, _vp]),
+    ("qmiv_loss_backward", c_i32, [_vp, _vp, c_i32, c_i32, c_i32, _P(Options), _vp, ctypes.c_size_t, _vp, _vp, _vp,
+                                   _vp]),
     ("qmiv_finish_sequence", c_i32, [_vp, _P(SeqResult)]),
     ("qmiv_reset_sequence", c_i32, [_vp]),
     ("qmiv_kernel_launches", ctypes.c_int64, [_vp]),

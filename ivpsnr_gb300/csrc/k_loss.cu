@@ -1,0 +1,410 @@
+// Differentiable IV-PSNR error and IV-SSIM of FP32 4:4:4 pictures with values in [0, 1]
+// (Max = 1), batched over n picture pairs laid out [n][3][H][W]. The reference takes integer
+// samples only; its definitions carry over without the integer rounding:
+//   GCD_c   = clip(mean(R_c - T_c), -u_c, u_c)                  (xGlobClrDiff.cpp:15-48)
+//   R2T:  s1(p) = argmin_s sum_c w_c (T_c(p) + GCD_c - R_c(p+s))^2, first strict minimum in
+//         row-major order over the (2B+1)^2 window, coordinates clamped at the borders
+//         (xCorrespPixelShift.cpp:48-85); e1_c(p) = T_c(p) + GCD_c - R_c(p+s1(p))
+//   T2R:  s0(p) = argmin_s sum_c w_c (R_c(p) - GCD_c - T_c(p+s))^2;  e0_c = R_c(p) - GCD_c - T_c(p+s0)
+//   SSE_c(R2T) = sum e1_c^2, SSE_c(T2R) = sum e0_c^2                 (xIVPSNR.cpp:62-95)
+//   SCP1_c = clip(R_c(p+s1) - GCD_c, 0, 1), SCP0_c = clip(T_c(p+s0) + GCD_c, 0, 1)  (xShftCompPic.cpp:69-96)
+//   SSIM_c(T2R) = SSIM(T_c, SCP1_c), SSIM_c(R2T) = SSIM(R_c, SCP0_c)   (xSSIM.cpp:166-190)
+// Gradients with respect to T: the argmin is piecewise constant (no gradient), the error at
+// the argmin routes to the pixel it was read from (gather for R2T, scatter for T2R, done here
+// as a gather over the window so that it is deterministic), clips pass gradient inside
+// [lo, hi] inclusive, and GCD contributes -1/Area per pixel while it is not clipped.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "qmiv_device.cuh"
+#include "qmiv_loss.h"
+
+namespace qmiv {
+
+namespace {
+
+constexpr int kCpsTX = 32, kCpsTY = 8;
+
+struct Geo {
+  const float* tst;
+  const float* ref;
+  int n, W, H;
+  int64_t plane;       // W*H
+};
+
+// ---- global colour difference ---------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_loss_gcd_part(Geo g, double* __restrict__ part)
+{
+  __shared__ double scratch[16];
+  const int pc = blockIdx.y;                         // image*3 + component
+  const int64_t per = (g.plane + kLossGcdChunks - 1) / kLossGcdChunks;
+  const int64_t b0 = (int64_t)blockIdx.x * per, b1 = min(g.plane, b0 + per);
+  const float* r = g.ref + (int64_t)pc * g.plane;
+  const float* t = g.tst + (int64_t)pc * g.plane;
+  Kbns k = { 0.0, 0.0 };
+  for(int64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) k = kbns_add(k, (double)__ldg(r + i) - (double)__ldg(t + i));
+  const double s = block_kbns(k, scratch);
+  if(threadIdx.x == 0) part[pc * kLossGcdChunks + blockIdx.x] = s;
+}
+
+__global__ void k_loss_gcd_final(Geo g, const double* __restrict__ part, float unc0, float unc1, float unc2,
+                                 float* __restrict__ gcd, int* __restrict__ ok)
+{
+  const int pc = blockIdx.x * blockDim.x + threadIdx.x;
+  if(pc >= g.n * 3) return;
+  Kbns k = { 0.0, 0.0 };
+  for(int i = 0; i < kLossGcdChunks; i++) k = kbns_add(k, part[pc * kLossGcdChunks + i]);
+  const float m = (float)(kbns_result(k) / (double)g.plane);
+  const int c = pc % 3;
+  const float u = c == 0 ? unc0 : (c == 1 ? unc1 : unc2);
+  gcd[pc] = fminf(fmaxf(m, -u), u);
+  ok[pc] = (m >= -u && m <= u) ? 1 : 0;  // clip passes gradient on [-u, u] inclusive
+}
+
+// ---- corresponding-pixel search, both directions ----------------------------------------------
+__device__ __forceinline__ float werr(float d0, float d1, float d2, float w0, float w1, float w2)
+{ // ((w0 d0^2) + (w1 d1^2)) + (w2 d2^2), no contraction: the same rounding as separate tensor ops
+  return __fadd_rn(__fadd_rn(__fmul_rn(w0, __fmul_rn(d0, d0)), __fmul_rn(w1, __fmul_rn(d1, d1))), __fmul_rn(w2, __fmul_rn(d2, d2)));
+}
+
+template <int SR>
+__global__ void __launch_bounds__(kCpsTX * kCpsTY) k_loss_cps(Geo g, float w0, float w1, float w2,
+                                                              const float* __restrict__ gcd, uint16_t* __restrict__ maps,
+                                                              float* __restrict__ scp, double* __restrict__ sse_part,
+                                                              int blocks_per_image)
+{
+  constexpr int SWX = kCpsTX + 2 * SR, SWY = kCpsTY + 2 * SR;
+  __shared__ float s_t[3][SWY][SWX], s_r[3][SWY][SWX];
+  __shared__ float s_red[8][6];
+  const int b = blockIdx.y;
+  const int bx = blockIdx.x % ((g.W + kCpsTX - 1) / kCpsTX), by = blockIdx.x / ((g.W + kCpsTX - 1) / kCpsTX);
+  const int x0 = bx * kCpsTX, y0 = by * kCpsTY;
+  const float* T = g.tst + (int64_t)b * 3 * g.plane;
+  const float* R = g.ref + (int64_t)b * 3 * g.plane;
+  for(int i = threadIdx.x; i < 3 * SWY * SWX; i += blockDim.x)
+  {
+    const int c = i / (SWY * SWX), rr = (i / SWX) % SWY, q = i % SWX;
+    const int gx = min(max(x0 - SR + q, 0), g.W - 1), gy = min(max(y0 - SR + rr, 0), g.H - 1);
+    const int64_t o = (int64_t)c * g.plane + (int64_t)gy * g.W + gx;
+    s_t[c][rr][q] = __ldg(T + o);
+    s_r[c][rr][q] = __ldg(R + o);
+  }
+  __syncthreads();
+  const int lx = threadIdx.x % kCpsTX, ly = threadIdx.x / kCpsTX;
+  const int x = x0 + lx, y = y0 + ly;
+  const bool inside = x < g.W && y < g.H;
+  float e1[3] = { 0.f, 0.f, 0.f }, e0[3] = { 0.f, 0.f, 0.f };
+  if(inside)
+  {
+    float gc[3], tg[3], rg[3];
+    for(int c = 0; c < 3; c++)
+    {
+      gc[c] = gcd[b * 3 + c];
+      tg[c] = __fadd_rn(s_t[c][ly + SR][lx + SR], gc[c]);
+      rg[c] = __fsub_rn(s_r[c][ly + SR][lx + SR], gc[c]);
+    }
+    float best1 = INFINITY, best0 = INFINITY;
+    int k1 = 0, k0 = 0;
+    #pragma unroll
+    for(int dy = 0; dy <= 2 * SR; dy++)
+      #pragma unroll
+      for(int dx = 0; dx <= 2 * SR; dx++)
+      {
+        // clamped candidate (x+dx-SR, y+dy-SR) in staged coordinates
+        const int cx = min(max(x + dx - SR, 0), g.W - 1) - x0 + SR;
+        const int cy = min(max(y + dy - SR, 0), g.H - 1) - y0 + SR;
+        const float E1 = werr(__fsub_rn(tg[0], s_r[0][cy][cx]), __fsub_rn(tg[1], s_r[1][cy][cx]), __fsub_rn(tg[2], s_r[2][cy][cx]), w0, w1, w2);
+        const float E0 = werr(__fsub_rn(rg[0], s_t[0][cy][cx]), __fsub_rn(rg[1], s_t[1][cy][cx]), __fsub_rn(rg[2], s_t[2][cy][cx]), w0, w1, w2);
+        const int k = dy * (2 * SR + 1) + dx;
+        if(E1 < best1) { best1 = E1; k1 = k; }
+        if(E0 < best0) { best0 = E0; k0 = k; }
+      }
+    const int c1x = min(max(x + k1 % (2 * SR + 1) - SR, 0), g.W - 1) - x0 + SR, c1y = min(max(y + k1 / (2 * SR + 1) - SR, 0), g.H - 1) - y0 + SR;
+    const int c0x = min(max(x + k0 % (2 * SR + 1) - SR, 0), g.W - 1) - x0 + SR, c0y = min(max(y + k0 / (2 * SR + 1) - SR, 0), g.H - 1) - y0 + SR;
+    int m1 = k1, m0 = k0;
+    const int64_t pix = (int64_t)y * g.W + x;
+    float* scp1 = scp + (int64_t)b * 3 * g.plane;
+    float* scp0 = scp + ((int64_t)g.n + b) * 3 * g.plane;
+    for(int c = 0; c < 3; c++)
+    {
+      const float rv = s_r[c][c1y][c1x], tv = s_t[c][c0y][c0x];
+      e1[c] = __fsub_rn(tg[c], rv);
+      e0[c] = __fsub_rn(rg[c], tv);
+      const float a1 = __fsub_rn(rv, gc[c]), a0 = __fadd_rn(tv, gc[c]);
+      if(a1 >= 0.f && a1 <= 1.f) m1 |= 256 << c;
+      if(a0 >= 0.f && a0 <= 1.f) m0 |= 256 << c;
+      scp1[(int64_t)c * g.plane + pix] = fminf(fmaxf(a1, 0.f), 1.f);
+      scp0[(int64_t)c * g.plane + pix] = fminf(fmaxf(a0, 0.f), 1.f);
+    }
+    maps[(int64_t)b * g.plane + pix] = (uint16_t)m1;
+    maps[((int64_t)g.n + b) * g.plane + pix] = (uint16_t)m0;
+  }
+  // per-block SSE partials: [R2T c0..2, T2R c0..2]
+  float v[6] = { e1[0] * e1[0], e1[1] * e1[1], e1[2] * e1[2], e0[0] * e0[0], e0[1] * e0[1], e0[2] * e0[2] };
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for(int i = 0; i < 6; i++)
+  {
+    const float s = warp_sum(v[i]);
+    if(lane == 0) s_red[warp][i] = s;
+  }
+  __syncthreads();
+  if(threadIdx.x < 6)
+  {
+    double s = 0.0;
+    for(int w = 0; w < 8; w++) s += (double)s_red[w][threadIdx.x];
+    const int d = threadIdx.x / 3, c = threadIdx.x % 3;
+    sse_part[(((int64_t)b * 2 + d) * 3 + c) * blocks_per_image + blockIdx.x] = s;
+  }
+}
+
+// sum of per-block partials: out[i] = sum_k part[i][k] (fixed order), one warp per output
+__global__ void k_loss_sum_parts(const double* __restrict__ part, int nparts, int nout, double* __restrict__ out,
+                                 double scale)
+{
+  const int i = blockIdx.x;
+  if(i >= nout) return;
+  Kbns k = { 0.0, 0.0 };
+  for(int j = threadIdx.x; j < nparts; j += 32) k = kbns_add(k, part[(int64_t)i * nparts + j]);
+  k = warp_kbns(k);
+  if(threadIdx.x == 0) out[i] = kbns_result(k) * scale;
+}
+
+// ---- backward -------------------------------------------------------------------------------
+struct BwdArgs {
+  Geo g;
+  int sr;
+  const float* gcd;
+  const int* gcd_ok;
+  const uint16_t* maps;      // [2][n][H][W]: argmin index (bits 0-7), unclipped SCP (bits 8-10)
+  const float* dy;           // [2][n][3][H][W]: T2R then R2T
+  const double* g_sse;       // [n][2][3]
+  double* g_part;            // [n*3][blocks]
+  const double* g_gcd;       // [n*3] (combine pass)
+  float* g_tst;
+  int blocks_per_image;
+};
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// Partial sums of d loss / d GCD_c over the pixels of one 32x8 block.
+__global__ void __launch_bounds__(256) k_loss_gcd_grad_part(BwdArgs a)
+{
+  __shared__ double scratch[16];
+  const Geo& g = a.g;
+  const int b = blockIdx.y, side = 2 * a.sr + 1;
+  const int tiles_x = (g.W + kCpsTX - 1) / kCpsTX;
+  const int x = (blockIdx.x % tiles_x) * kCpsTX + (threadIdx.x % kCpsTX);
+  const int y = (blockIdx.x / tiles_x) * kCpsTY + (threadIdx.x / kCpsTX);
+  const bool inside = x < g.W && y < g.H;
+  const float* T = g.tst + (int64_t)b * 3 * g.plane;
+  const float* R = g.ref + (int64_t)b * 3 * g.plane;
+  const int64_t pix = (int64_t)y * g.W + x;
+  int m1 = 0, m0 = 0, q1 = 0, q0 = 0;
+  if(inside)
+  {
+    m1 = a.maps[(int64_t)b * g.plane + pix];
+    m0 = a.maps[((int64_t)g.n + b) * g.plane + pix];
+    const int k1 = m1 & 255, k0 = m0 & 255;
+    q1 = clampi(y + k1 / side - a.sr, 0, g.H - 1) * g.W + clampi(x + k1 % side - a.sr, 0, g.W - 1);
+    q0 = clampi(y + k0 / side - a.sr, 0, g.H - 1) * g.W + clampi(x + k0 % side - a.sr, 0, g.W - 1);
+  }
+  for(int c = 0; c < 3; c++)
+  {
+    double v = 0.0;
+    if(inside)
+    {
+      const float gc = a.gcd[b * 3 + c];
+      const float e1 = __fsub_rn(__fadd_rn(T[(int64_t)c * g.plane + pix], gc), R[(int64_t)c * g.plane + q1]);
+      const float e0 = __fsub_rn(__fsub_rn(R[(int64_t)c * g.plane + pix], gc), T[(int64_t)c * g.plane + q0]);
+      const double gs1 = a.g_sse[(b * 2 + 0) * 3 + c], gs0 = a.g_sse[(b * 2 + 1) * 3 + c];
+      v = 2.0 * gs1 * (double)e1 - 2.0 * gs0 * (double)e0;
+      const float dyt = a.dy[((int64_t)b * 3 + c) * g.plane + pix];                      // T2R: d/dSCP1
+      const float dyr = a.dy[(((int64_t)g.n + b) * 3 + c) * g.plane + pix];              // R2T: d/dSCP0
+      if(m1 & (256 << c)) v -= (double)dyt;
+      if(m0 & (256 << c)) v += (double)dyr;
+    }
+    Kbns k = { v, 0.0 };
+    const double s = block_kbns(k, scratch);
+    if(threadIdx.x == 0) a.g_part[((int64_t)b * 3 + c) * a.blocks_per_image + blockIdx.x] = s;
+  }
+}
+
+// d loss / d T(q): the SSIM T2R term already in g_tst, plus the R2T error at q, plus every T2R
+// error and R2T SCP sample read from q (gathered over the window), plus the GCD term.
+__global__ void __launch_bounds__(256) k_loss_grad(BwdArgs a)
+{
+  const Geo& g = a.g;
+  const int b = blockIdx.y, side = 2 * a.sr + 1;
+  const int tiles_x = (g.W + kCpsTX - 1) / kCpsTX;
+  const int x = (blockIdx.x % tiles_x) * kCpsTX + (threadIdx.x % kCpsTX);
+  const int y = (blockIdx.x / tiles_x) * kCpsTY + (threadIdx.x / kCpsTX);
+  if(x >= g.W || y >= g.H) return;
+  const float* T = g.tst + (int64_t)b * 3 * g.plane;
+  const float* R = g.ref + (int64_t)b * 3 * g.plane;
+  const int64_t q = (int64_t)y * g.W + x;
+  const int m1 = a.maps[(int64_t)b * g.plane + q], k1 = m1 & 255;
+  const int q1 = clampi(y + k1 / side - a.sr, 0, g.H - 1) * g.W + clampi(x + k1 % side - a.sr, 0, g.W - 1);
+  float acc[3];
+  float gc[3];
+  for(int c = 0; c < 3; c++)
+  {
+    gc[c] = a.gcd[b * 3 + c];
+    const float e1 = __fsub_rn(__fadd_rn(T[(int64_t)c * g.plane + q], gc[c]), R[(int64_t)c * g.plane + q1]);
+    acc[c] = a.g_tst[((int64_t)b * 3 + c) * g.plane + q] + (float)(2.0 * a.g_sse[(b * 2 + 0) * 3 + c]) * e1;
+  }
+  // pixels p whose T2R argmin reads q: p within the window around q
+  for(int dy = -a.sr; dy <= a.sr; dy++)
+    for(int dx = -a.sr; dx <= a.sr; dx++)
+    {
+      const int px = x + dx, py = y + dy;
+      if(px < 0 || px >= g.W || py < 0 || py >= g.H) continue;
+      const int64_t p = (int64_t)py * g.W + px;
+      const int m0 = a.maps[((int64_t)g.n + b) * g.plane + p], k0 = m0 & 255;
+      const int tx = clampi(px + k0 % side - a.sr, 0, g.W - 1), ty = clampi(py + k0 / side - a.sr, 0, g.H - 1);
+      if(tx != x || ty != y) continue;
+      for(int c = 0; c < 3; c++)
+      {
+        const float e0 = __fsub_rn(__fsub_rn(R[(int64_t)c * g.plane + p], gc[c]), T[(int64_t)c * g.plane + q]);
+        float v = (float)(-2.0 * a.g_sse[(b * 2 + 1) * 3 + c]) * e0;
+        if(m0 & (256 << c)) v += a.dy[(((int64_t)g.n + b) * 3 + c) * g.plane + p];
+        acc[c] += v;
+      }
+    }
+  for(int c = 0; c < 3; c++)
+  {
+    if(a.gcd_ok[b * 3 + c]) acc[c] -= (float)(a.g_gcd[b * 3 + c] / (double)g.plane);
+    a.g_tst[((int64_t)b * 3 + c) * g.plane + q] = acc[c];
+  }
+}
+
+size_t al256(size_t v) { return (v + 255) & ~(size_t)255; }
+
+}  // namespace
+
+LossLayout loss_layout(int n, int W, int H, int window)
+{
+  LossLayout L;
+  std::memset(&L, 0, sizeof(L));
+  L.n = n; L.W = W; L.H = H; L.window = window;
+  L.tiles_x = ssim_tiles_x(W, window);
+  L.tiles_y = ssim_tiles_y(H);
+  L.cps_blocks = ((W + kCpsTX - 1) / kCpsTX) * ((H + kCpsTY - 1) / kCpsTY);
+  const size_t plane = (size_t)W * H;
+  size_t o = 0;
+  L.gcd_part = o; o += al256(sizeof(double) * n * 3 * kLossGcdChunks);
+  L.gcd = o;      o += al256(sizeof(float) * n * 3) + al256(sizeof(int) * n * 3);
+  L.maps = o;     o += al256(sizeof(uint16_t) * 2 * (size_t)n * plane);
+  L.scp = o;      o += al256(sizeof(float) * 2 * (size_t)n * 3 * plane);
+  L.sse_part = o; o += al256(sizeof(double) * (size_t)n * 6 * L.cps_blocks);
+  L.sjobs = o;    o += al256(std::max(sizeof(SsimJob), sizeof(SsimBwdJob)) * n * 6);
+  L.partial = o;  o += al256(sizeof(float) * (size_t)n * 6 * std::max(0, H - 10) * L.tiles_x);
+  L.dy = o;       o += al256(sizeof(float) * 2 * (size_t)n * 3 * plane);
+  L.g_part = o;   o += al256(sizeof(double) * (size_t)n * 3 * L.cps_blocks) + al256(sizeof(double) * n * 3);
+  L.bytes = o;
+  return L;
+}
+
+cudaError_t loss_forward(const LossArgs& a, double* sse, double* ssim, cudaStream_t st)
+{
+  const LossLayout& L = a.L;
+  Geo g = { a.tst, a.ref, a.n, a.W, a.H, (int64_t)a.W * a.H };
+  double* gpart = (double*)(a.ws + L.gcd_part);
+  float* gcd = (float*)(a.ws + L.gcd);
+  int* ok = (int*)(a.ws + L.gcd + al256(sizeof(float) * a.n * 3));
+  uint16_t* maps = (uint16_t*)(a.ws + L.maps);
+  float* scp = (float*)(a.ws + L.scp);
+  double* ssep = (double*)(a.ws + L.sse_part);
+  k_loss_gcd_part<<<dim3(kLossGcdChunks, a.n * 3), 256, 0, st>>>(g, gpart);
+  k_loss_gcd_final<<<(a.n * 3 + 63) / 64, 64, 0, st>>>(g, gpart, a.unc[0], a.unc[1], a.unc[2], gcd, ok);
+  const dim3 grid(L.cps_blocks, a.n);
+  switch(a.sr)
+  {
+    case 1: k_loss_cps<1><<<grid, kCpsTX * kCpsTY, 0, st>>>(g, a.w_search[0], a.w_search[1], a.w_search[2], gcd, maps, scp, ssep, L.cps_blocks); break;
+    case 2: k_loss_cps<2><<<grid, kCpsTX * kCpsTY, 0, st>>>(g, a.w_search[0], a.w_search[1], a.w_search[2], gcd, maps, scp, ssep, L.cps_blocks); break;
+    case 3: k_loss_cps<3><<<grid, kCpsTX * kCpsTY, 0, st>>>(g, a.w_search[0], a.w_search[1], a.w_search[2], gcd, maps, scp, ssep, L.cps_blocks); break;
+    default: k_loss_cps<4><<<grid, kCpsTX * kCpsTY, 0, st>>>(g, a.w_search[0], a.w_search[1], a.w_search[2], gcd, maps, scp, ssep, L.cps_blocks); break;
+  }
+  k_loss_sum_parts<<<a.n * 6, 32, 0, st>>>(ssep, L.cps_blocks, a.n * 6, sse, 1.0);
+  // SSIM jobs: (b, d, c) -> ssim[b][d][c]; d 0 = R2T: SSIM(R, SCP0), d 1 = T2R: SSIM(T, SCP1)
+  std::vector<SsimJob> jobs(a.n * 6);
+  const size_t plane = (size_t)a.W * a.H;
+  float* part = (float*)(a.ws + L.partial);
+  int base = 0;
+  for(int b = 0; b < a.n; b++)
+    for(int d = 0; d < 2; d++)
+      for(int c = 0; c < 3; c++)
+      {
+        SsimJob& j = jobs[(b * 2 + d) * 3 + c];
+        std::memset(&j, 0, sizeof(j));
+        const float* first = (d == 0 ? a.ref : a.tst) + ((size_t)b * 3 + c) * plane;
+        const float* second = scp + (((size_t)(d == 0 ? a.n : 0) + b) * 3 + c) * plane;
+        j.a.ptr = first; j.a.stride = a.W; j.a.sbytes = 4; j.a.shift = 0;
+        j.b.ptr = second; j.b.stride = a.W; j.b.sbytes = 4; j.b.shift = 0;
+        j.W = a.W; j.H = a.H; j.calc_l = 1;
+        j.c1 = 0.01f * 0.01f; j.c2 = 0.03f * 0.03f;
+        j.tiles_x = L.tiles_x; j.tiles_y = L.tiles_y; j.tile_base = base;
+        base += L.tiles_x * L.tiles_y;
+        j.partial = part + (size_t)((b * 2 + d) * 3 + c) * std::max(0, a.H - 10) * L.tiles_x;
+        j.out = ssim + (b * 2 + d) * 3 + c;
+      }
+  SsimJob* d_jobs = (SsimJob*)(a.ws + L.sjobs);
+  cudaError_t e = cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(SsimJob) * jobs.size(), cudaMemcpyHostToDevice, st);
+  if(e != cudaSuccess) return e;
+  e = launch_ssim(d_jobs, jobs.data(), (int)jobs.size(), a.window, st);
+  if(e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+cudaError_t loss_backward(const LossArgs& a, const double* g_sse, const double* g_ssim, float* g_tst, cudaStream_t st)
+{
+  const LossLayout& L = a.L;
+  Geo g = { a.tst, a.ref, a.n, a.W, a.H, (int64_t)a.W * a.H };
+  const size_t plane = (size_t)a.W * a.H;
+  float* scp = (float*)(a.ws + L.scp);
+  float* dy = (float*)(a.ws + L.dy);
+  // SSIM backward: T2R (d 1) writes d/dT into g_tst and d/dSCP1 into dy[0]; R2T (d 0) writes d/dSCP0 into dy[1]
+  std::vector<SsimBwdJob> jobs;
+  int base = 0;
+  const int tx = ssim_bwd_tiles(a.W), ty = ssim_bwd_tiles(a.H);
+  for(int b = 0; b < a.n; b++)
+    for(int d = 0; d < 2; d++)
+      for(int c = 0; c < 3; c++)
+      {
+        SsimBwdJob j;
+        std::memset(&j, 0, sizeof(j));
+        const size_t pl = ((size_t)b * 3 + c) * plane;
+        j.a.ptr = (d == 0 ? a.ref : a.tst) + pl; j.a.stride = a.W; j.a.sbytes = 4;
+        j.b.ptr = scp + (((size_t)(d == 0 ? a.n : 0) + b) * 3 + c) * plane; j.b.stride = a.W; j.b.sbytes = 4;
+        j.W = a.W; j.H = a.H; j.c1 = 0.01f * 0.01f; j.c2 = 0.03f * 0.03f;
+        j.tiles_x = tx; j.tiles_y = ty; j.tile_base = base; base += tx * ty;
+        j.g = g_ssim + (b * 2 + d) * 3 + c;
+        j.outx = d == 1 ? g_tst + pl : nullptr;
+        j.outy = dy + (((size_t)(d == 1 ? 0 : a.n) + b) * 3 + c) * plane;
+        jobs.push_back(j);
+      }
+  SsimBwdJob* d_jobs = (SsimBwdJob*)(a.ws + L.sjobs);
+  cudaError_t e = cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(SsimBwdJob) * jobs.size(), cudaMemcpyHostToDevice, st);
+  if(e != cudaSuccess) return e;
+  e = launch_ssim_bwd(d_jobs, jobs.data(), (int)jobs.size(), a.window, st);
+  if(e != cudaSuccess) return e;
+  BwdArgs ba;
+  ba.g = g; ba.sr = a.sr;
+  ba.gcd = (const float*)(a.ws + L.gcd);
+  ba.gcd_ok = (const int*)(a.ws + L.gcd + al256(sizeof(float) * a.n * 3));
+  ba.maps = (const uint16_t*)(a.ws + L.maps);
+  ba.dy = dy;
+  ba.g_sse = g_sse;
+  ba.g_part = (double*)(a.ws + L.g_part);
+  double* g_gcd = (double*)(a.ws + L.g_part + al256(sizeof(double) * (size_t)a.n * 3 * L.cps_blocks));
+  ba.g_gcd = g_gcd;
+  ba.g_tst = g_tst;
+  ba.blocks_per_image = L.cps_blocks;
+  const dim3 grid(L.cps_blocks, a.n);
+  k_loss_gcd_grad_part<<<grid, kCpsTX * kCpsTY, 0, st>>>(ba);
+  k_loss_sum_parts<<<a.n * 3, 32, 0, st>>>(ba.g_part, L.cps_blocks, a.n * 3, g_gcd, 1.0);
+  k_loss_grad<<<grid, kCpsTX * kCpsTY, 0, st>>>(ba);
+  return cudaGetLastError();
+}
+
+}  // namespace qmiv

@@ -49,7 +49,14 @@ template <int WIN> struct SGeo {
   static_assert(8 * 7 >= TX && 8 * 6 + 7 + WIN - 1 < kRP, "tile columns");
 };
 
-__device__ __forceinline__ int ld_plane(const SsimPlane& p, int x, int y)
+__device__ __forceinline__ float ld_plane(const SsimPlane& p, int x, int y)
+{
+  const int64_t o = (int64_t)(y >> p.shift) * p.stride + (x >> p.shift);
+  if(p.sbytes == 4) return __ldg((const float*)p.ptr + o);
+  return p.sbytes == 1 ? (float)__ldg((const uint8_t*)p.ptr + o) : (float)__ldg((const uint16_t*)p.ptr + o);
+}
+
+__device__ __forceinline__ int ld_int(const SsimPlane& p, int x, int y)
 {
   const int64_t o = (int64_t)(y >> p.shift) * p.stride + (x >> p.shift);
   return p.sbytes == 1 ? (int)__ldg((const uint8_t*)p.ptr + o) : (int)__ldg((const uint16_t*)p.ptr + o);
@@ -57,9 +64,9 @@ __device__ __forceinline__ int ld_plane(const SsimPlane& p, int x, int y)
 
 // One plane's part of a staged tile, in registers: warp w takes staged rows w, w+8, ...,
 // lanes the staged columns lane and lane+32. Rows and columns past the picture clamp (they
-// only feed outputs outside the valid region).
+// only feed outputs outside the valid region). Integer samples convert exactly.
 template <typename T, int SH, int IH>
-__device__ __forceinline__ void load_rows(const SsimPlane& P, int (&v)[(IH + 7) / 8][2], int xs, int ys, int W, int H)
+__device__ __forceinline__ void load_rows(const SsimPlane& P, float (&v)[(IH + 7) / 8][2], int xs, int ys, int W, int H)
 {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const T* base = reinterpret_cast<const T*>(P.ptr);
@@ -69,16 +76,17 @@ __device__ __forceinline__ void load_rows(const SsimPlane& P, int (&v)[(IH + 7) 
   {
     const int i = min(warp + 8 * k, IH - 1);
     const T* row = base + (int64_t)(min(ys + i, H - 1) >> SH) * P.stride;
-    v[k][0] = __ldg(row + gx0);
-    v[k][1] = __ldg(row + gx1);
+    v[k][0] = (float)__ldg(row + gx0);
+    v[k][1] = (float)__ldg(row + gx1);
   }
 }
 
 template <int IH>
-__device__ __forceinline__ void load_plane(const SsimPlane& P, int (&v)[(IH + 7) / 8][2], int xs, int ys, int W, int H)
+__device__ __forceinline__ void load_plane(const SsimPlane& P, float (&v)[(IH + 7) / 8][2], int xs, int ys, int W, int H)
 {
-  if(P.sbytes == 1) { if(P.shift) load_rows<uint8_t, 1, IH>(P, v, xs, ys, W, H); else load_rows<uint8_t, 0, IH>(P, v, xs, ys, W, H); }
-  else              { if(P.shift) load_rows<uint16_t, 1, IH>(P, v, xs, ys, W, H); else load_rows<uint16_t, 0, IH>(P, v, xs, ys, W, H); }
+  if(P.sbytes == 4)      load_rows<float, 0, IH>(P, v, xs, ys, W, H);
+  else if(P.sbytes == 1) { if(P.shift) load_rows<uint8_t, 1, IH>(P, v, xs, ys, W, H); else load_rows<uint8_t, 0, IH>(P, v, xs, ys, W, H); }
+  else                   { if(P.shift) load_rows<uint16_t, 1, IH>(P, v, xs, ys, W, H); else load_rows<uint16_t, 0, IH>(P, v, xs, ys, W, H); }
 }
 
 // Where tile `tile` is: its job (found by a forward scan from jb) and its origin.
@@ -126,8 +134,8 @@ __global__ void __launch_bounds__(kThreads, 3) k_ssim(const SsimJob* __restrict_
     const int x1 = min(x0 + G::TX, J.W - 5), y1 = min(y0 + kTY, J.H - 5);
 
     // staging: centring offset c = the tile-centre sample of plane b, loaded with the tile
-    int va[G::RPW][2], vb[G::RPW][2];
-    const int tc = ld_plane(J.b, min((x0 + x1) >> 1, J.W - 1), min((y0 + y1) >> 1, J.H - 1));
+    float va[G::RPW][2], vb[G::RPW][2];
+    const float tc = ld_plane(J.b, min((x0 + x1) >> 1, J.W - 1), min((y0 + y1) >> 1, J.H - 1));
     load_plane<G::IH>(J.a, va, x0 - 5, y0 - 5, J.W, J.H);
     load_plane<G::IH>(J.b, vb, x0 - 5, y0 - 5, J.W, J.H);
     #pragma unroll
@@ -191,7 +199,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_ssim(const SsimJob* __restrict_
           m2[jj] = __ffma2_rn(gk[k], hi2(val), m2[jj]);
         }
       }
-      const float cf = (float)tc;
+      const float cf = tc;
       const float k_cc = (float)(c_omd[wi] * (double)tc * (double)tc * c_w0d[wi]);
       const float cw0 = cf * c_w0[wi], om2c = c_om[wi] * 2.0f * cf, omc = c_om[wi] * cf;
       const float vq0 = 2.0f * k_cc + J.c2, cv0 = k_cc, C1 = J.c1, C2 = J.c2;
@@ -258,7 +266,7 @@ __global__ void __launch_bounds__(256) k_downsample(const PyrStep* __restrict__ 
   {
     if(x >= S.dw) break;
     const int sx = 2 * x, sy = 2 * y;
-    const int v = ld_plane(S.src, sx, sy) + ld_plane(S.src, sx + 1, sy) + ld_plane(S.src, sx, sy + 1) + ld_plane(S.src, sx + 1, sy + 1);
+    const int v = ld_int(S.src, sx, sy) + ld_int(S.src, sx + 1, sy) + ld_int(S.src, sx, sy + 1) + ld_int(S.src, sx + 1, sy + 1);
     S.dst[(int64_t)y * S.dst_stride + x] = (uint16_t)((v + 2) >> 2);
   }
 }
@@ -300,6 +308,142 @@ __global__ void k_ssim_combine(const SsimFrame* __restrict__ frames, int nframes
     R->ivssim_t2r = a;
     R->ivssim_r2t = b;
     R->ivssim = b < a ? b : a; // std::min(SSIM_T2R, SSIM_R2T) (xSSIM.cpp:205)
+  }
+}
+
+// ---- backward ---------------------------------------------------------------------------
+// d SSIM / d a(q) and d SSIM / d b(q) for every sample q of two FP32 planes. SSIM is the mean
+// over the valid region of s(p) = L(p) CS(p), built from the raw window moments
+// mu_a = sum w a, E_aa = sum w a^2, E_bb, E_ab (var = E - mu^2, cov = E_ab - mu_a mu_b). With
+//   B = ds/dE_aa = ds/dE_bb = -L CS / D2,  C = ds/dE_ab = 2 L / D2,
+//   A_a = ds/dmu_a = CS (2 mu_b - 2 mu_a L) / D1 - 2 mu_a B - mu_b C  (and A_b symmetric),
+// the chain rule gives d SSIM / d a(q) = (1/WH) sum_p w(q-p) [A_a(p) + 2 a(q) B(p) + b(q) C(p)],
+// i.e. the coefficient maps filtered with the window and combined with the samples at q.
+// Statistics are recomputed from the pictures (nothing is stored by the forward pass). Samples
+// are centred by the tile-centre value c as in the forward kernel; the combination uses centred
+// samples with A'' = A + c (2B + C).
+constexpr int kBwdT = 32;  // output tile 32 x 32
+template <int WIN> struct BGeo {
+  static constexpr int PW = kBwdT + WIN - 1;        // window positions p whose map reaches the tile
+  static constexpr int SW = PW + WIN - 1;           // staged samples
+  static constexpr int SMEM = SW * SW * 8 + PW * SW * 16 + PW * PW * 16;
+};
+
+template <int WIN>
+__global__ void __launch_bounds__(256) k_ssim_bwd(const SsimBwdJob* __restrict__ jobs, int njobs)
+{
+  using G = BGeo<WIN>;
+  constexpr int PW = G::PW, SW = G::SW;
+  extern __shared__ __align__(16) float smem[];
+  float2* s_in = reinterpret_cast<float2*>(smem);                   // [SW][SW] centred (a, b)
+  float4* s_v = reinterpret_cast<float4*>(smem + 2 * SW * SW);      // [PW][SW] vertical sums; later [32][PW]
+  float4* s_m = s_v + PW * SW;                                      // [PW][PW] coefficient maps
+  int jb = 0;
+  { int lo = 0, hi = njobs - 1;
+    while(lo < hi) { const int mid = (lo + hi + 1) >> 1; if(jobs[mid].tile_base <= (int)blockIdx.x) lo = mid; else hi = mid - 1; }
+    jb = lo; }
+  const SsimBwdJob& J = jobs[jb];
+  const int local = blockIdx.x - J.tile_base;
+  const int ty = local / J.tiles_x, tx = local - ty * J.tiles_x;
+  const int W = J.W, H = J.H, tid = threadIdx.x;
+  const int qx0 = tx * kBwdT, qy0 = ty * kBwdT;
+  const int px0 = qx0 - (WIN - 6), py0 = qy0 - (WIN - 6);  // p = q - k, k in [-5, WIN-6]
+  const int sx0 = px0 - 5, sy0 = py0 - 5;
+  const float c = __ldg((const float*)J.b.ptr + (int64_t)min(qy0 + kBwdT / 2, H - 1) * J.b.stride + min(qx0 + kBwdT / 2, W - 1));
+  const float* pa = (const float*)J.a.ptr;
+  const float* pb = (const float*)J.b.ptr;
+  for(int i = tid; i < SW * SW; i += 256)
+  {
+    const int r = i / SW, q = i - r * SW;
+    const int gx = min(max(sx0 + q, 0), W - 1), gy = min(max(sy0 + r, 0), H - 1);
+    s_in[i] = make_float2(__ldg(pa + (int64_t)gy * J.a.stride + gx) - c, __ldg(pb + (int64_t)gy * J.b.stride + gx) - c);
+  }
+  __syncthreads();
+  // vertical window sums for every p row and staged column
+  for(int i = tid; i < PW * SW; i += 256)
+  {
+    const int r = i / SW, q = i - r * SW;
+    float4 m = make_float4(0.f, 0.f, 0.f, 0.f);
+    #pragma unroll
+    for(int k = 0; k < WIN; k++)
+    {
+      const float2 v = s_in[(r + k) * SW + q];
+      const float g = c_g[k];
+      m.x = fmaf(g, v.x, m.x); m.y = fmaf(g, v.y, m.y);
+      m.z = fmaf(g, fmaf(v.x, v.x, v.y * v.y), m.z); m.w = fmaf(g, v.x * v.y, m.w);
+    }
+    s_v[i] = m;
+  }
+  __syncthreads();
+  // horizontal sums -> moments at p -> coefficient maps (zero outside the valid region)
+  const int wi = WIN == 11 ? 1 : 0;
+  const float w0 = c_w0[wi], om = c_om[wi];
+  const float k_cc = (float)(c_omd[wi] * (double)c * (double)c * c_w0d[wi]);
+  const float C1 = J.c1, C2 = J.c2;
+  for(int i = tid; i < PW * PW; i += 256)
+  {
+    const int r = i / PW, q = i - r * PW;
+    const int px = px0 + q, py = py0 + r;
+    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+    if(px >= 5 && px < W - 5 && py >= 5 && py < H - 5)
+    {
+      float4 m = make_float4(0.f, 0.f, 0.f, 0.f);
+      #pragma unroll
+      for(int k = 0; k < WIN; k++)
+      {
+        const float4 v = s_v[r * SW + q + k];
+        const float g = c_g[k];
+        m.x = fmaf(g, v.x, m.x); m.y = fmaf(g, v.y, m.y); m.z = fmaf(g, v.z, m.z); m.w = fmaf(g, v.w, m.w);
+      }
+      const float S1a = m.x, S1b = m.y, sab = S1a + S1b;
+      const float mua = S1a + c * w0, mub = S1b + c * w0;
+      const float vsum = fmaf(-S1b, S1b, fmaf(-S1a, S1a, m.z)) + fmaf(om * 2.0f * c, sab, 2.0f * k_cc);
+      const float cov = fmaf(-S1a, S1b, m.w) + fmaf(om * c, sab, k_cc);
+      const float N1 = fmaf(2.0f * mua, mub, C1), D1 = fmaf(mua, mua, fmaf(mub, mub, C1));
+      const float N2 = fmaf(2.0f, cov, C2), D2 = vsum + C2;
+      const float L = N1 / D1, CS = N2 / D2;
+      const float B = -L * CS / D2, Cc = 2.0f * L / D2;
+      const float Aa = CS * (2.0f * mub - 2.0f * mua * L) / D1 - 2.0f * mua * B - mub * Cc;
+      const float Ab = CS * (2.0f * mua - 2.0f * mub * L) / D1 - 2.0f * mub * B - mua * Cc;
+      const float cc = c * (2.0f * B + Cc);
+      out = make_float4(Aa + cc, Ab + cc, B, Cc);
+    }
+    s_m[i] = out;
+  }
+  __syncthreads();
+  // transposed vertical pass: F[qr][pc] = sum_j g[j] M[qr + WIN-1-j][pc]  (reuses s_v)
+  float4* s_f = s_v;
+  for(int i = tid; i < kBwdT * PW; i += 256)
+  {
+    const int r = i / PW, q = i - r * PW;
+    float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+    #pragma unroll
+    for(int j = 0; j < WIN; j++)
+    {
+      const float4 v = s_m[(r + WIN - 1 - j) * PW + q];
+      const float g = c_g[j];
+      f.x = fmaf(g, v.x, f.x); f.y = fmaf(g, v.y, f.y); f.z = fmaf(g, v.z, f.z); f.w = fmaf(g, v.w, f.w);
+    }
+    s_f[i] = f;
+  }
+  __syncthreads();
+  const float scale = (float)(*J.g / ((double)W * (double)H));
+  for(int i = tid; i < kBwdT * kBwdT; i += 256)
+  {
+    const int r = i >> 5, q = i & 31;
+    const int x = qx0 + q, y = qy0 + r;
+    if(x >= W || y >= H) continue;
+    float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+    #pragma unroll
+    for(int j = 0; j < WIN; j++)
+    {
+      const float4 v = s_f[r * PW + q + WIN - 1 - j];
+      const float g = c_g[j];
+      f.x = fmaf(g, v.x, f.x); f.y = fmaf(g, v.y, f.y); f.z = fmaf(g, v.z, f.z); f.w = fmaf(g, v.w, f.w);
+    }
+    const float2 v = s_in[(r + WIN - 1) * SW + (q + WIN - 1)];  // the centred samples at q
+    if(J.outx) J.outx[(int64_t)y * W + x] = scale * (f.x + 2.0f * v.x * f.z + v.y * f.w);
+    if(J.outy) J.outy[(int64_t)y * W + x] = scale * (f.y + 2.0f * v.y * f.z + v.x * f.w);
   }
 }
 
@@ -357,6 +501,26 @@ cudaError_t launch_ssim(const SsimJob* d_jobs, const SsimJob* h_jobs, int n, int
     if(e != cudaSuccess) return e;
   }
   k_ssim_finalize<<<n, 256, 0, st>>>(d_jobs, n);
+  return cudaGetLastError();
+}
+
+int ssim_bwd_tiles(int dim) { return (dim + kBwdT - 1) / kBwdT; }
+
+cudaError_t launch_ssim_bwd(const SsimBwdJob* d_jobs, const SsimBwdJob* h_jobs, int n, int window, cudaStream_t st)
+{
+  int blocks = 0;
+  for(int i = 0; i < n; i++) blocks = h_jobs[i].tile_base + h_jobs[i].tiles_x * h_jobs[i].tiles_y;
+  if(blocks == 0) return cudaSuccess;
+  static bool attr = false;
+  if(!attr)
+  {
+    cudaError_t e = cudaFuncSetAttribute(k_ssim_bwd<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, BGeo<10>::SMEM);
+    if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_bwd<11>, cudaFuncAttributeMaxDynamicSharedMemorySize, BGeo<11>::SMEM);
+    if(e != cudaSuccess) return e;
+    attr = true;
+  }
+  if(window == QMIV_SSIM_GAUSS11) k_ssim_bwd<11><<<blocks, 256, BGeo<11>::SMEM, st>>>(d_jobs, n);
+  else                            k_ssim_bwd<10><<<blocks, 256, BGeo<10>::SMEM, st>>>(d_jobs, n);
   return cudaGetLastError();
 }
 

@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -15,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include "qmiv_internal.h"
+#include "qmiv_loss.h"
 #include "qmiv_ssim.h"
 
 using namespace qmiv;
@@ -1196,3 +1198,76 @@ qmiv_status qmiv_reset_sequence(qmiv_handle* h)
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------------------
+// Differentiable IV-PSNR error and IV-SSIM on FP32 4:4:4 pictures (k_loss.cu)
+// ------------------------------------------------------------------------------------
+namespace {
+
+std::mutex g_const_mu;
+bool g_const_set[kStaticMaxDevices] = { false };
+
+qmiv_status loss_args(const float* tst, const float* ref, int32_t n, int32_t w, int32_t h, const qmiv_options* opt,
+                      void* ws, size_t ws_bytes, LossArgs& a)
+{
+  qmiv_options o;
+  if(opt) o = *opt; else qmiv_default_options(&o);
+  qmiv_status s = check_options(&o);
+  if(s != QMIV_OK) return s;
+  if(n < 1 || w < 1 || h < 1) return fail(QMIV_BAD_ARG, "loss: n %d, size %dx%d", n, w, h);
+  if(o.search_range < 1 || o.search_range > kLossMaxSR)
+    return fail(QMIV_UNSUPPORTED, "loss: search_range %d (1..%d)", o.search_range, kLossMaxSR);
+  if(!tst || !ref) return fail(QMIV_BAD_ARG, "loss: null picture");
+  a.tst = tst; a.ref = ref; a.n = n; a.W = w; a.H = h; a.sr = o.search_range;
+  for(int c = 0; c < 3; c++) { a.w_search[c] = (float)o.cmp_w_search[c]; a.unc[c] = o.unnoticeable[c]; }
+  a.window = o.ssim_window;
+  a.L = loss_layout(n, w, h, o.ssim_window);
+  a.ws = (uint8_t*)ws;
+  if(ws_bytes < a.L.bytes) return fail(QMIV_BAD_ARG, "loss: workspace %zu B < %zu B", ws_bytes, a.L.bytes);
+  if(!ws || ((uintptr_t)ws & 255)) return fail(QMIV_BAD_ARG, "loss: workspace must be 256-byte aligned device memory");
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  if(dev < 0 || dev >= kStaticMaxDevices) return fail(QMIV_CUDA_ERROR, "loss: device %d", dev);
+  std::lock_guard<std::mutex> lock(g_const_mu);
+  if(!g_const_set[dev])
+  {
+    CUDA_TRY(set_ssim_constants());
+    g_const_set[dev] = true;
+  }
+  return QMIV_OK;
+}
+
+}  // namespace
+
+qmiv_status qmiv_loss_workspace_size(int32_t n, int32_t width, int32_t height, const qmiv_options* opt, size_t* bytes)
+{
+  if(!bytes || n < 1 || width < 1 || height < 1) return fail(QMIV_BAD_ARG, "loss workspace: bad arguments");
+  qmiv_options o;
+  if(opt) o = *opt; else qmiv_default_options(&o);
+  *bytes = loss_layout(n, width, height, o.ssim_window).bytes;
+  return QMIV_OK;
+}
+
+qmiv_status qmiv_loss_forward(const float* tst, const float* ref, int32_t n, int32_t width, int32_t height,
+                              const qmiv_options* opt, void* workspace, size_t workspace_bytes, double* sse,
+                              double* ssim, qmiv_stream stream)
+{
+  LossArgs a;
+  qmiv_status s = loss_args(tst, ref, n, width, height, opt, workspace, workspace_bytes, a);
+  if(s != QMIV_OK) return s;
+  if(!sse || !ssim) return fail(QMIV_BAD_ARG, "loss: null outputs");
+  CUDA_TRY(loss_forward(a, sse, ssim, (cudaStream_t)stream));
+  return QMIV_OK;
+}
+
+qmiv_status qmiv_loss_backward(const float* tst, const float* ref, int32_t n, int32_t width, int32_t height,
+                               const qmiv_options* opt, void* workspace, size_t workspace_bytes, const double* g_sse,
+                               const double* g_ssim, float* g_tst, qmiv_stream stream)
+{
+  LossArgs a;
+  qmiv_status s = loss_args(tst, ref, n, width, height, opt, workspace, workspace_bytes, a);
+  if(s != QMIV_OK) return s;
+  if(!g_sse || !g_ssim || !g_tst) return fail(QMIV_BAD_ARG, "loss: null gradients");
+  CUDA_TRY(loss_backward(a, g_sse, g_ssim, g_tst, (cudaStream_t)stream));
+  return QMIV_OK;
+}

@@ -47,6 +47,20 @@ struct SsimFrame {
 
 constexpr int kSsimVals = 24;
 
+// One SSIM backward evaluation: gradients of g * SSIM(a, b) (the picture mean of the SSIM map,
+// L*CS) with respect to every sample of a and of b, over the whole picture. Planes are FP32.
+struct SsimBwdJob {
+  SsimPlane a, b;
+  int32_t W, H;
+  float c1, c2;
+  int32_t tiles_x, tiles_y, tile_base;
+  const double* g;       // upstream gradient of this SSIM value
+  float* outx;           // d/da, W x H with row pitch W (null: not needed)
+  float* outy;           // d/db (null: not needed)
+};
+int ssim_bwd_tiles(int dim);
+cudaError_t launch_ssim_bwd(const SsimBwdJob* d_jobs, const SsimBwdJob* h_jobs, int n, int window, cudaStream_t st);
+
 cudaError_t ssim_set_window_constants(const float g[11], const double w0[2]);
 int ssim_tiles_x(int W, int window);
 int ssim_tiles_y(int H);
