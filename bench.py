@@ -240,6 +240,74 @@ def ssim_workload(args, dev, stream):
             "check": {"ivssim_frame0": r0.ivssim, "ssim_frame0": list(r0.ssim)[:3]}}
 
 
+LOSS_WORKLOAD = ("ivssim-ivpsnr-loss-fwd-bwd: 16 x FP32 4:4:4 1024x1024 in [0,1], tested = reference + N(0, 0.02^2)"
+                 " + per-channel offset + block shifts, SR 2, REF10 window")
+
+
+def loss_workload(args, dev):
+    """Differentiable IV-PSNR error + IV-SSIM: forward and backward of
+    loss = mean(1 - IV-SSIM) - 0.01 mean(IV-PSNR dB) over a batch of 16 FP32 1024x1024 pictures,
+    through ivpsnr_gb300.loss (the library's kernels), next to the same loss written in plain
+    torch ops (tests/loss_reference.py, FP32 autograd) on the same GPU."""
+    import torch
+    from ivpsnr_gb300 import loss, synth
+    n, w, h = 16, 1024, 1024
+    rs, ts = [], []
+    for i in range(n):
+        r, t = synth.float444(w, h, seed=synth.seed_for(3, 0, i))
+        rs.append(torch.from_numpy(r))
+        ts.append(torch.from_numpy(t))
+    ref = torch.stack(rs).to(dev)
+    tst = torch.stack(ts).to(dev).requires_grad_(True)
+    area = w * h
+
+    def objective(sse, ss):
+        return (1.0 - loss.ivssim(ss)).mean() - 0.01 * loss.ivpsnr_db(sse, area).mean()
+
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+
+    def time_it(fwd):
+        for _ in range(args.warmup):
+            tst.grad = None
+            objective(*fwd()).backward()
+        torch.cuda.synchronize()
+        f_ms = b_ms = 0.0
+        for _ in range(args.steps):
+            tst.grad = None
+            e[0].record()
+            L = objective(*fwd())
+            e[1].record()
+            L.backward()
+            e[2].record()
+            torch.cuda.synchronize()
+            f_ms += e[0].elapsed_time(e[1])
+            b_ms += e[1].elapsed_time(e[2])
+        return f_ms / args.steps, b_ms / args.steps
+
+    f_ms, b_ms = time_it(lambda: loss.iv_metrics(tst, ref))
+    out = {"workload": LOSS_WORKLOAD, "fwd_ms": f_ms, "bwd_ms": b_ms, "fwd_bwd_ms": f_ms + b_ms,
+           "value": n * area / ((f_ms + b_ms) * 1e-3) / 1e9, "unit": "Gpixel/s (fwd+bwd)"}
+    if args.kernels_only:
+        del tst, ref
+        torch.cuda.empty_cache()
+        return out
+    try:
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import loss_reference as plain
+
+        def plain_fwd():
+            sse, ss, _ = plain.forward(tst, ref)
+            return sse, ss
+        pf, pb = time_it(plain_fwd)
+        out["plain_autograd"] = {"fwd_ms": pf, "bwd_ms": pb, "fwd_bwd_ms": pf + pb,
+                                 "speedup": (pf + pb) / (f_ms + b_ms)}
+    except Exception as ex:  # out of memory or missing torch feature: report, do not fail the bench
+        out["plain_autograd"] = {"unavailable": str(ex)[:200]}
+    del tst, ref
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -254,6 +322,11 @@ def run_ours(args):
     dev = torch.device("cuda", local)
     if args.workload == "ssim":
         r = ssim_workload(args, dev, torch.cuda.current_stream(dev))
+        if rank == 0:
+            print(json.dumps(r))
+        return
+    if args.workload == "loss":
+        r = loss_workload(args, dev)
         if rank == 0:
             print(json.dumps(r))
         return
@@ -403,6 +476,7 @@ def run_ours(args):
     torch.cuda.empty_cache()
 
     ssim_line = None if args.skip_ssim else ssim_workload(args, dev, stream)
+    loss_line = None if args.skip_loss else loss_workload(args, dev)
 
     if rank == 0:
         line = {
@@ -428,6 +502,8 @@ def run_ours(args):
         }
         if ssim_line:
             line["ivssim"] = ssim_line
+        if loss_line:
+            line["loss"] = loss_line
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_sample()
         print(json.dumps(line))
@@ -442,9 +518,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="multiview", choices=["multiview", "small", "ssim"],
+    ap.add_argument("--workload", default="multiview", choices=["multiview", "small", "ssim", "loss"],
                     help="small: the 24-pair 1080p case used for ncu captures")
     ap.add_argument("--skip-ssim", action="store_true", help="skip the IV-SSIM / SSIM / MS-SSIM workload")
+    ap.add_argument("--skip-loss", action="store_true", help="skip the differentiable-loss forward/backward workload")
     ap.add_argument("--kernels-only", action="store_true",
                     help="time only the batched launches (for profiler captures)")
     args = ap.parse_args()

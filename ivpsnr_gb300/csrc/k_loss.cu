@@ -42,8 +42,9 @@ __global__ void __launch_bounds__(256) k_loss_gcd_part(Geo g, double* __restrict
   const int64_t b0 = (int64_t)blockIdx.x * per, b1 = min(g.plane, b0 + per);
   const float* r = g.ref + (int64_t)pc * g.plane;
   const float* t = g.tst + (int64_t)pc * g.plane;
-  Kbns k = { 0.0, 0.0 };
-  for(int64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) k = kbns_add(k, (double)__ldg(r + i) - (double)__ldg(t + i));
+  double acc = 0.0;  // FP32 differences are exact in FP64; a thread adds a few hundred of them
+  for(int64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) acc += (double)__ldg(r + i) - (double)__ldg(t + i);
+  Kbns k = { acc, 0.0 };
   const double s = block_kbns(k, scratch);
   if(threadIdx.x == 0) part[pc * kLossGcdChunks + blockIdx.x] = s;
 }
@@ -82,13 +83,27 @@ __global__ void __launch_bounds__(kCpsTX * kCpsTY) k_loss_cps(Geo g, float w0, f
   const int x0 = bx * kCpsTX, y0 = by * kCpsTY;
   const float* T = g.tst + (int64_t)b * 3 * g.plane;
   const float* R = g.ref + (int64_t)b * 3 * g.plane;
-  for(int i = threadIdx.x; i < 3 * SWY * SWX; i += blockDim.x)
-  {
-    const int c = i / (SWY * SWX), rr = (i / SWX) % SWY, q = i % SWX;
-    const int gx = min(max(x0 - SR + q, 0), g.W - 1), gy = min(max(y0 - SR + rr, 0), g.H - 1);
-    const int64_t o = (int64_t)c * g.plane + (int64_t)gy * g.W + gx;
-    s_t[c][rr][q] = __ldg(T + o);
-    s_r[c][rr][q] = __ldg(R + o);
+  { // all loads of the tile are issued before the first store
+    constexpr int N = 3 * SWY * SWX, NI = (N + kCpsTX * kCpsTY - 1) / (kCpsTX * kCpsTY);
+    float vt[NI], vr[NI];
+    #pragma unroll
+    for(int k = 0; k < NI; k++)
+    {
+      const int i = min((int)threadIdx.x + kCpsTX * kCpsTY * k, N - 1);
+      const int c = i / (SWY * SWX), rr = (i / SWX) % SWY, q = i % SWX;
+      const int gx = min(max(x0 - SR + q, 0), g.W - 1), gy = min(max(y0 - SR + rr, 0), g.H - 1);
+      const int64_t o = (int64_t)c * g.plane + (int64_t)gy * g.W + gx;
+      vt[k] = __ldg(T + o);
+      vr[k] = __ldg(R + o);
+    }
+    #pragma unroll
+    for(int k = 0; k < NI; k++)
+    {
+      const int i = threadIdx.x + kCpsTX * kCpsTY * k;
+      if(i >= N) break;
+      (&s_t[0][0][0])[i] = vt[k];
+      (&s_r[0][0][0])[i] = vr[k];
+    }
   }
   __syncthreads();
   const int lx = threadIdx.x % kCpsTX, ly = threadIdx.x / kCpsTX;
@@ -187,12 +202,15 @@ struct BwdArgs {
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
-// Partial sums of d loss / d GCD_c over the pixels of one 32x8 block.
+// Partial sums of d loss / d GCD_c over the pixels of one 32x8 block (FP32 within the block,
+// FP64 across blocks).
+template <int SR>
 __global__ void __launch_bounds__(256) k_loss_gcd_grad_part(BwdArgs a)
 {
-  __shared__ double scratch[16];
+  __shared__ float s_red[8][3];
   const Geo& g = a.g;
-  const int b = blockIdx.y, side = 2 * a.sr + 1;
+  constexpr int side = 2 * SR + 1;
+  const int b = blockIdx.y;
   const int tiles_x = (g.W + kCpsTX - 1) / kCpsTX;
   const int x = (blockIdx.x % tiles_x) * kCpsTX + (threadIdx.x % kCpsTX);
   const int y = (blockIdx.x / tiles_x) * kCpsTY + (threadIdx.x / kCpsTX);
@@ -200,82 +218,109 @@ __global__ void __launch_bounds__(256) k_loss_gcd_grad_part(BwdArgs a)
   const float* T = g.tst + (int64_t)b * 3 * g.plane;
   const float* R = g.ref + (int64_t)b * 3 * g.plane;
   const int64_t pix = (int64_t)y * g.W + x;
-  int m1 = 0, m0 = 0, q1 = 0, q0 = 0;
+  float v[3] = { 0.f, 0.f, 0.f };
   if(inside)
   {
-    m1 = a.maps[(int64_t)b * g.plane + pix];
-    m0 = a.maps[((int64_t)g.n + b) * g.plane + pix];
+    const int m1 = a.maps[(int64_t)b * g.plane + pix];
+    const int m0 = a.maps[((int64_t)g.n + b) * g.plane + pix];
     const int k1 = m1 & 255, k0 = m0 & 255;
-    q1 = clampi(y + k1 / side - a.sr, 0, g.H - 1) * g.W + clampi(x + k1 % side - a.sr, 0, g.W - 1);
-    q0 = clampi(y + k0 / side - a.sr, 0, g.H - 1) * g.W + clampi(x + k0 % side - a.sr, 0, g.W - 1);
-  }
-  for(int c = 0; c < 3; c++)
-  {
-    double v = 0.0;
-    if(inside)
+    const int64_t q1 = (int64_t)clampi(y + k1 / side - SR, 0, g.H - 1) * g.W + clampi(x + k1 % side - SR, 0, g.W - 1);
+    const int64_t q0 = (int64_t)clampi(y + k0 / side - SR, 0, g.H - 1) * g.W + clampi(x + k0 % side - SR, 0, g.W - 1);
+    #pragma unroll
+    for(int c = 0; c < 3; c++)
     {
       const float gc = a.gcd[b * 3 + c];
       const float e1 = __fsub_rn(__fadd_rn(T[(int64_t)c * g.plane + pix], gc), R[(int64_t)c * g.plane + q1]);
       const float e0 = __fsub_rn(__fsub_rn(R[(int64_t)c * g.plane + pix], gc), T[(int64_t)c * g.plane + q0]);
-      const double gs1 = a.g_sse[(b * 2 + 0) * 3 + c], gs0 = a.g_sse[(b * 2 + 1) * 3 + c];
-      v = 2.0 * gs1 * (double)e1 - 2.0 * gs0 * (double)e0;
-      const float dyt = a.dy[((int64_t)b * 3 + c) * g.plane + pix];                      // T2R: d/dSCP1
-      const float dyr = a.dy[(((int64_t)g.n + b) * 3 + c) * g.plane + pix];              // R2T: d/dSCP0
-      if(m1 & (256 << c)) v -= (double)dyt;
-      if(m0 & (256 << c)) v += (double)dyr;
+      const float gs1 = (float)a.g_sse[(b * 2 + 0) * 3 + c], gs0 = (float)a.g_sse[(b * 2 + 1) * 3 + c];
+      float t = 2.0f * (gs1 * e1 - gs0 * e0);
+      if(m1 & (256 << c)) t -= a.dy[((int64_t)b * 3 + c) * g.plane + pix];            // T2R: d/dSCP1
+      if(m0 & (256 << c)) t += a.dy[(((int64_t)g.n + b) * 3 + c) * g.plane + pix];    // R2T: d/dSCP0
+      v[c] = t;
     }
-    Kbns k = { v, 0.0 };
-    const double s = block_kbns(k, scratch);
-    if(threadIdx.x == 0) a.g_part[((int64_t)b * 3 + c) * a.blocks_per_image + blockIdx.x] = s;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  #pragma unroll
+  for(int c = 0; c < 3; c++)
+  {
+    const float s = warp_sum(v[c]);
+    if(lane == 0) s_red[warp][c] = s;
+  }
+  __syncthreads();
+  if(threadIdx.x < 3)
+  {
+    double s = 0.0;
+    for(int w = 0; w < 8; w++) s += (double)s_red[w][threadIdx.x];
+    a.g_part[((int64_t)b * 3 + threadIdx.x) * a.blocks_per_image + blockIdx.x] = s;
   }
 }
 
 // d loss / d T(q): the SSIM T2R term already in g_tst, plus the R2T error at q, plus every T2R
 // error and R2T SCP sample read from q (gathered over the window), plus the GCD term.
+template <int SR>
 __global__ void __launch_bounds__(256) k_loss_grad(BwdArgs a)
 {
+  constexpr int HW = kCpsTX + 2 * kLossMaxSR, HH = kCpsTY + 2 * kLossMaxSR;
+  __shared__ uint16_t s_m0[HH][HW];
+  __shared__ float s_f[4][3];   // 2 g_sse(R2T), -2 g_sse(T2R), -g_gcd/area (or 0 when clipped)
   const Geo& g = a.g;
-  const int b = blockIdx.y, side = 2 * a.sr + 1;
+  constexpr int side = 2 * SR + 1, sr = SR;
+  const int b = blockIdx.y;
   const int tiles_x = (g.W + kCpsTX - 1) / kCpsTX;
-  const int x = (blockIdx.x % tiles_x) * kCpsTX + (threadIdx.x % kCpsTX);
-  const int y = (blockIdx.x / tiles_x) * kCpsTY + (threadIdx.x / kCpsTX);
+  const int x0 = (blockIdx.x % tiles_x) * kCpsTX, y0 = (blockIdx.x / tiles_x) * kCpsTY;
+  const uint16_t* m0map = a.maps + ((int64_t)g.n + b) * g.plane;
+  for(int i = threadIdx.x; i < HH * HW; i += blockDim.x)
+  {
+    const int r = i / HW, q = i % HW;
+    const int px = x0 - kLossMaxSR + q, py = y0 - kLossMaxSR + r;
+    // outside the picture: an index that never maps back into the tile
+    s_m0[r][q] = (px >= 0 && px < g.W && py >= 0 && py < g.H) ? m0map[(int64_t)py * g.W + px] : (uint16_t)0xffffu;
+  }
+  if(threadIdx.x < 3)
+  {
+    const int c = threadIdx.x;
+    s_f[0][c] = (float)(2.0 * a.g_sse[(b * 2 + 0) * 3 + c]);
+    s_f[1][c] = (float)(-2.0 * a.g_sse[(b * 2 + 1) * 3 + c]);
+    s_f[2][c] = a.gcd_ok[b * 3 + c] ? (float)(-a.g_gcd[b * 3 + c] / (double)g.plane) : 0.0f;
+    s_f[3][c] = a.gcd[b * 3 + c];
+  }
+  __syncthreads();
+  const int lx = threadIdx.x % kCpsTX, ly = threadIdx.x / kCpsTX;
+  const int x = x0 + lx, y = y0 + ly;
   if(x >= g.W || y >= g.H) return;
   const float* T = g.tst + (int64_t)b * 3 * g.plane;
   const float* R = g.ref + (int64_t)b * 3 * g.plane;
   const int64_t q = (int64_t)y * g.W + x;
-  const int m1 = a.maps[(int64_t)b * g.plane + q], k1 = m1 & 255;
-  const int q1 = clampi(y + k1 / side - a.sr, 0, g.H - 1) * g.W + clampi(x + k1 % side - a.sr, 0, g.W - 1);
-  float acc[3];
-  float gc[3];
+  const int k1 = a.maps[(int64_t)b * g.plane + q] & 255;
+  const int64_t q1 = (int64_t)clampi(y + k1 / side - sr, 0, g.H - 1) * g.W + clampi(x + k1 % side - sr, 0, g.W - 1);
+  float acc[3], tq[3];
+  #pragma unroll
   for(int c = 0; c < 3; c++)
   {
-    gc[c] = a.gcd[b * 3 + c];
-    const float e1 = __fsub_rn(__fadd_rn(T[(int64_t)c * g.plane + q], gc[c]), R[(int64_t)c * g.plane + q1]);
-    acc[c] = a.g_tst[((int64_t)b * 3 + c) * g.plane + q] + (float)(2.0 * a.g_sse[(b * 2 + 0) * 3 + c]) * e1;
+    tq[c] = T[(int64_t)c * g.plane + q];
+    const float e1 = __fsub_rn(__fadd_rn(tq[c], s_f[3][c]), R[(int64_t)c * g.plane + q1]);
+    acc[c] = a.g_tst[((int64_t)b * 3 + c) * g.plane + q] + s_f[0][c] * e1 + s_f[2][c];
   }
-  // pixels p whose T2R argmin reads q: p within the window around q
-  for(int dy = -a.sr; dy <= a.sr; dy++)
-    for(int dx = -a.sr; dx <= a.sr; dx++)
+  // pixels p whose T2R argmin reads q lie within the window around q
+  for(int dy = -sr; dy <= sr; dy++)
+    for(int dx = -sr; dx <= sr; dx++)
     {
-      const int px = x + dx, py = y + dy;
-      if(px < 0 || px >= g.W || py < 0 || py >= g.H) continue;
+      const int m0 = s_m0[ly + kLossMaxSR + dy][lx + kLossMaxSR + dx];
+      if(m0 == 0xffff) continue;
+      const int k0 = m0 & 255, px = x + dx, py = y + dy;
+      if(clampi(px + k0 % side - sr, 0, g.W - 1) != x || clampi(py + k0 / side - sr, 0, g.H - 1) != y) continue;
       const int64_t p = (int64_t)py * g.W + px;
-      const int m0 = a.maps[((int64_t)g.n + b) * g.plane + p], k0 = m0 & 255;
-      const int tx = clampi(px + k0 % side - a.sr, 0, g.W - 1), ty = clampi(py + k0 / side - a.sr, 0, g.H - 1);
-      if(tx != x || ty != y) continue;
+      #pragma unroll
       for(int c = 0; c < 3; c++)
       {
-        const float e0 = __fsub_rn(__fsub_rn(R[(int64_t)c * g.plane + p], gc[c]), T[(int64_t)c * g.plane + q]);
-        float v = (float)(-2.0 * a.g_sse[(b * 2 + 1) * 3 + c]) * e0;
+        const float e0 = __fsub_rn(__fsub_rn(R[(int64_t)c * g.plane + p], s_f[3][c]), tq[c]);
+        float v = s_f[1][c] * e0;
         if(m0 & (256 << c)) v += a.dy[(((int64_t)g.n + b) * 3 + c) * g.plane + p];
         acc[c] += v;
       }
     }
-  for(int c = 0; c < 3; c++)
-  {
-    if(a.gcd_ok[b * 3 + c]) acc[c] -= (float)(a.g_gcd[b * 3 + c] / (double)g.plane);
-    a.g_tst[((int64_t)b * 3 + c) * g.plane + q] = acc[c];
-  }
+  #pragma unroll
+  for(int c = 0; c < 3; c++) a.g_tst[((int64_t)b * 3 + c) * g.plane + q] = acc[c];
 }
 
 size_t al256(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -401,9 +446,21 @@ cudaError_t loss_backward(const LossArgs& a, const double* g_sse, const double* 
   ba.g_tst = g_tst;
   ba.blocks_per_image = L.cps_blocks;
   const dim3 grid(L.cps_blocks, a.n);
-  k_loss_gcd_grad_part<<<grid, kCpsTX * kCpsTY, 0, st>>>(ba);
+  switch(a.sr)
+  {
+    case 1: k_loss_gcd_grad_part<1><<<grid, kCpsTX * kCpsTY, 0, st>>>(ba); break;
+    case 2: k_loss_gcd_grad_part<2><<<grid, kCpsTX * kCpsTY, 0, st>>>(ba); break;
+    case 3: k_loss_gcd_grad_part<3><<<grid, kCpsTX * kCpsTY, 0, st>>>(ba); break;
+    default: k_loss_gcd_grad_part<4><<<grid, kCpsTX * kCpsTY, 0, st>>>(ba); break;
+  }
   k_loss_sum_parts<<<a.n * 3, 32, 0, st>>>(ba.g_part, L.cps_blocks, a.n * 3, g_gcd, 1.0);
-  k_loss_grad<<<grid, kCpsTX * kCpsTY, 0, st>>>(ba);
+  switch(a.sr)
+  {
+    case 1: k_loss_grad<1><<<grid, kCpsTX * kCpsTY, 0, st>>>(ba); break;
+    case 2: k_loss_grad<2><<<grid, kCpsTX * kCpsTY, 0, st>>>(ba); break;
+    case 3: k_loss_grad<3><<<grid, kCpsTX * kCpsTY, 0, st>>>(ba); break;
+    default: k_loss_grad<4><<<grid, kCpsTX * kCpsTY, 0, st>>>(ba); break;
+  }
   return cudaGetLastError();
 }
 

@@ -326,18 +326,41 @@ constexpr int kBwdT = 32;  // output tile 32 x 32
 template <int WIN> struct BGeo {
   static constexpr int PW = kBwdT + WIN - 1;        // window positions p whose map reaches the tile
   static constexpr int SW = PW + WIN - 1;           // staged samples
-  static constexpr int SMEM = SW * SW * 8 + PW * SW * 16 + PW * PW * 16;
+  // row pitches (float4) read down a column by consecutive lanes are odd: conflict-free
+  static constexpr int VP = SW | 1, MP = PW | 1;
+  // region A: staged samples [SW][SW] float2, later the coefficient maps [PW][MP] float4;
+  // region B: vertical sums [PW][VP] float4, later F [32][MP] float4; the tile's own centred
+  // samples [32][32] float2
+  static constexpr int A = (SW * SW * 8 > PW * MP * 16 ? SW * SW * 8 : PW * MP * 16);
+  static constexpr int B = PW * VP * 16;
+  static constexpr int SMEM = A + B + kBwdT * kBwdT * 8;
+  static_assert(kBwdT * MP <= PW * VP, "F aliases V");
 };
 
+// acc += g * v on a float4 as two packed FP32 multiply-adds
+__device__ __forceinline__ void fma4(float2 g, const float4& v, float4& acc)
+{
+  const float2 lo = __ffma2_rn(g, make_float2(v.x, v.y), make_float2(acc.x, acc.y));
+  const float2 hi = __ffma2_rn(g, make_float2(v.z, v.w), make_float2(acc.z, acc.w));
+  acc = make_float4(lo.x, lo.y, hi.x, hi.y);
+}
+
+// Each pass is register-blocked: a thread filters 8 consecutive outputs along the pass
+// direction from 8 + WIN - 1 shared-memory reads.
 template <int WIN>
-__global__ void __launch_bounds__(256) k_ssim_bwd(const SsimBwdJob* __restrict__ jobs, int njobs)
+__global__ void __launch_bounds__(256, 3) k_ssim_bwd(const SsimBwdJob* __restrict__ jobs, int njobs)
 {
   using G = BGeo<WIN>;
-  constexpr int PW = G::PW, SW = G::SW;
+  constexpr int PW = G::PW, SW = G::SW, VP = G::VP, MP = G::MP, NG = (PW + 7) / 8;
   extern __shared__ __align__(16) float smem[];
-  float2* s_in = reinterpret_cast<float2*>(smem);                   // [SW][SW] centred (a, b)
-  float4* s_v = reinterpret_cast<float4*>(smem + 2 * SW * SW);      // [PW][SW] vertical sums; later [32][PW]
-  float4* s_m = s_v + PW * SW;                                      // [PW][PW] coefficient maps
+  float2* s_in = reinterpret_cast<float2*>(smem);                    // A: [SW][SW] centred a, b
+  float4* s_m = reinterpret_cast<float4*>(smem);                     // A: [PW][MP] coefficient maps
+  float4* s_v = reinterpret_cast<float4*>(smem + G::A / 4);          // B: [PW][VP] vertical sums
+  float4* s_f = s_v;                                                 // B: [32][MP]
+  float2* s_q = reinterpret_cast<float2*>(smem + (G::A + G::B) / 4); // [32][32] centred a, b at q
+  float2 gk[WIN];
+  #pragma unroll
+  for(int k = 0; k < WIN; k++) gk[k] = c_g2[k];
   int jb = 0;
   { int lo = 0, hi = njobs - 1;
     while(lo < hi) { const int mid = (lo + hi + 1) >> 1; if(jobs[mid].tile_base <= (int)blockIdx.x) lo = mid; else hi = mid - 1; }
@@ -352,98 +375,146 @@ __global__ void __launch_bounds__(256) k_ssim_bwd(const SsimBwdJob* __restrict__
   const float c = __ldg((const float*)J.b.ptr + (int64_t)min(qy0 + kBwdT / 2, H - 1) * J.b.stride + min(qx0 + kBwdT / 2, W - 1));
   const float* pa = (const float*)J.a.ptr;
   const float* pb = (const float*)J.b.ptr;
-  for(int i = tid; i < SW * SW; i += 256)
-  {
-    const int r = i / SW, q = i - r * SW;
-    const int gx = min(max(sx0 + q, 0), W - 1), gy = min(max(sy0 + r, 0), H - 1);
-    s_in[i] = make_float2(__ldg(pa + (int64_t)gy * J.a.stride + gx) - c, __ldg(pb + (int64_t)gy * J.b.stride + gx) - c);
-  }
-  __syncthreads();
-  // vertical window sums for every p row and staged column
-  for(int i = tid; i < PW * SW; i += 256)
-  {
-    const int r = i / SW, q = i - r * SW;
-    float4 m = make_float4(0.f, 0.f, 0.f, 0.f);
+  { // all loads of the tile are issued before the first store
+    constexpr int NI = (SW * SW + 255) / 256;
+    float va[NI], vb[NI];
     #pragma unroll
-    for(int k = 0; k < WIN; k++)
+    for(int k = 0; k < NI; k++)
     {
-      const float2 v = s_in[(r + k) * SW + q];
-      const float g = c_g[k];
-      m.x = fmaf(g, v.x, m.x); m.y = fmaf(g, v.y, m.y);
-      m.z = fmaf(g, fmaf(v.x, v.x, v.y * v.y), m.z); m.w = fmaf(g, v.x * v.y, m.w);
+      const int i = min(tid + 256 * k, SW * SW - 1);
+      const int r = i / SW, q = i - r * SW;
+      const int gx = min(max(sx0 + q, 0), W - 1), gy = min(max(sy0 + r, 0), H - 1);
+      va[k] = __ldg(pa + (int64_t)gy * J.a.stride + gx);
+      vb[k] = __ldg(pb + (int64_t)gy * J.b.stride + gx);
     }
-    s_v[i] = m;
+    #pragma unroll
+    for(int k = 0; k < NI; k++)
+    {
+      const int i = tid + 256 * k;
+      if(i >= SW * SW) break;
+      const float2 v = make_float2(va[k] - c, vb[k] - c);
+      s_in[i] = v;
+      const int r = i / SW - (WIN - 1), q = i % SW - (WIN - 1);  // staged (WIN-1, WIN-1) is q = (0, 0)
+      if(r >= 0 && r < kBwdT && q >= 0 && q < kBwdT) s_q[r * kBwdT + q] = v;
+    }
   }
   __syncthreads();
-  // horizontal sums -> moments at p -> coefficient maps (zero outside the valid region)
+  // vertical window sums: thread = staged column q x 8 consecutive p rows
+  for(int it = tid; it < SW * NG; it += 256)
+  {
+    const int q = it % SW, r0 = min(8 * (it / SW), PW - 8);
+    float4 acc[8];
+    #pragma unroll
+    for(int o = 0; o < 8; o++) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+    #pragma unroll
+    for(int i = 0; i < 7 + WIN; i++)
+    {
+      const float2 ab = s_in[(r0 + i) * SW + q];
+      const float4 v = make_float4(ab.x, ab.y, fmaf(ab.x, ab.x, ab.y * ab.y), ab.x * ab.y);
+      #pragma unroll
+      for(int o = 0; o < 8; o++)
+        if(i - o >= 0 && i - o < WIN) fma4(gk[i - o], v, acc[o]);
+    }
+    #pragma unroll
+    for(int o = 0; o < 8; o++) s_v[(r0 + o) * VP + q] = acc[o];
+  }
+  __syncthreads();
+  // horizontal sums -> moments at p -> coefficient maps (zero outside the valid region):
+  // thread = p row x 8 consecutive p columns
   const int wi = WIN == 11 ? 1 : 0;
   const float w0 = c_w0[wi], om = c_om[wi];
   const float k_cc = (float)(c_omd[wi] * (double)c * (double)c * c_w0d[wi]);
   const float C1 = J.c1, C2 = J.c2;
-  for(int i = tid; i < PW * PW; i += 256)
+  for(int it = tid; it < PW * NG; it += 256)
   {
-    const int r = i / PW, q = i - r * PW;
-    const int px = px0 + q, py = py0 + r;
-    float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
-    if(px >= 5 && px < W - 5 && py >= 5 && py < H - 5)
+    const int r = it % PW, c0 = min(8 * (it / PW), PW - 8);
+    float4 acc[8];
+    #pragma unroll
+    for(int o = 0; o < 8; o++) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+    #pragma unroll
+    for(int i = 0; i < 7 + WIN; i++)
     {
-      float4 m = make_float4(0.f, 0.f, 0.f, 0.f);
+      const float4 v = s_v[r * VP + c0 + i];
       #pragma unroll
-      for(int k = 0; k < WIN; k++)
+      for(int o = 0; o < 8; o++)
+        if(i - o >= 0 && i - o < WIN) fma4(gk[i - o], v, acc[o]);
+    }
+    const int py = py0 + r;
+    const bool row_ok = py >= 5 && py < H - 5;
+    #pragma unroll
+    for(int o = 0; o < 8; o++)
+    {
+      const int px = px0 + c0 + o;
+      float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+      if(row_ok && px >= 5 && px < W - 5)
       {
-        const float4 v = s_v[r * SW + q + k];
-        const float g = c_g[k];
-        m.x = fmaf(g, v.x, m.x); m.y = fmaf(g, v.y, m.y); m.z = fmaf(g, v.z, m.z); m.w = fmaf(g, v.w, m.w);
+        const float4 m = acc[o];
+        const float S1a = m.x, S1b = m.y, sab = S1a + S1b;
+        const float mua = S1a + c * w0, mub = S1b + c * w0;
+        const float vsum = fmaf(-S1b, S1b, fmaf(-S1a, S1a, m.z)) + fmaf(om * 2.0f * c, sab, 2.0f * k_cc);
+        const float cov = fmaf(-S1a, S1b, m.w) + fmaf(om * c, sab, k_cc);
+        const float N1 = fmaf(2.0f * mua, mub, C1), D1 = fmaf(mua, mua, fmaf(mub, mub, C1));
+        const float N2 = fmaf(2.0f, cov, C2), D2 = vsum + C2;
+        const float r1 = __fdividef(1.0f, D1), r2 = __fdividef(1.0f, D2);  // D1 >= C1, D2 ~ >= C2: far from 0
+        const float L = N1 * r1, CS = N2 * r2;
+        const float B = -L * CS * r2, Cc = 2.0f * L * r2;
+        const float Aa = CS * (2.0f * mub - 2.0f * mua * L) * r1 - 2.0f * mua * B - mub * Cc;
+        const float Ab = CS * (2.0f * mua - 2.0f * mub * L) * r1 - 2.0f * mub * B - mua * Cc;
+        const float cc = c * (2.0f * B + Cc);
+        out = make_float4(Aa + cc, Ab + cc, B, Cc);
       }
-      const float S1a = m.x, S1b = m.y, sab = S1a + S1b;
-      const float mua = S1a + c * w0, mub = S1b + c * w0;
-      const float vsum = fmaf(-S1b, S1b, fmaf(-S1a, S1a, m.z)) + fmaf(om * 2.0f * c, sab, 2.0f * k_cc);
-      const float cov = fmaf(-S1a, S1b, m.w) + fmaf(om * c, sab, k_cc);
-      const float N1 = fmaf(2.0f * mua, mub, C1), D1 = fmaf(mua, mua, fmaf(mub, mub, C1));
-      const float N2 = fmaf(2.0f, cov, C2), D2 = vsum + C2;
-      const float L = N1 / D1, CS = N2 / D2;
-      const float B = -L * CS / D2, Cc = 2.0f * L / D2;
-      const float Aa = CS * (2.0f * mub - 2.0f * mua * L) / D1 - 2.0f * mua * B - mub * Cc;
-      const float Ab = CS * (2.0f * mua - 2.0f * mub * L) / D1 - 2.0f * mub * B - mua * Cc;
-      const float cc = c * (2.0f * B + Cc);
-      out = make_float4(Aa + cc, Ab + cc, B, Cc);
+      s_m[r * MP + c0 + o] = out;
     }
-    s_m[i] = out;
   }
   __syncthreads();
-  // transposed vertical pass: F[qr][pc] = sum_j g[j] M[qr + WIN-1-j][pc]  (reuses s_v)
-  float4* s_f = s_v;
-  for(int i = tid; i < kBwdT * PW; i += 256)
+  // transposed vertical pass: F[qr][pc] = sum_j g[j] M[qr + WIN-1-j][pc];
+  // thread = p column x 8 consecutive q rows (F reuses the V area)
+  for(int it = tid; it < PW * (kBwdT / 8); it += 256)
   {
-    const int r = i / PW, q = i - r * PW;
-    float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int pc = it % PW, q0 = 8 * (it / PW);
+    float4 acc[8];
     #pragma unroll
-    for(int j = 0; j < WIN; j++)
+    for(int o = 0; o < 8; o++) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+    #pragma unroll
+    for(int i = 0; i < 7 + WIN; i++)
     {
-      const float4 v = s_m[(r + WIN - 1 - j) * PW + q];
-      const float g = c_g[j];
-      f.x = fmaf(g, v.x, f.x); f.y = fmaf(g, v.y, f.y); f.z = fmaf(g, v.z, f.z); f.w = fmaf(g, v.w, f.w);
+      const float4 v = s_m[(q0 + i) * MP + pc];
+      #pragma unroll
+      for(int o = 0; o < 8; o++)
+        if(o + WIN - 1 - i >= 0 && o + WIN - 1 - i < WIN) fma4(gk[o + WIN - 1 - i], v, acc[o]);
     }
-    s_f[i] = f;
+    #pragma unroll
+    for(int o = 0; o < 8; o++) s_f[(q0 + o) * MP + pc] = acc[o];
   }
   __syncthreads();
+  // transposed horizontal pass and the combination: thread = q row x 8 consecutive q columns
   const float scale = (float)(*J.g / ((double)W * (double)H));
-  for(int i = tid; i < kBwdT * kBwdT; i += 256)
+  for(int it = tid; it < kBwdT * (kBwdT / 8); it += 256)
   {
-    const int r = i >> 5, q = i & 31;
-    const int x = qx0 + q, y = qy0 + r;
-    if(x >= W || y >= H) continue;
-    float4 f = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int r = it % kBwdT, q0 = 8 * (it / kBwdT);
+    const int y = qy0 + r;
+    float4 acc[8];
     #pragma unroll
-    for(int j = 0; j < WIN; j++)
+    for(int o = 0; o < 8; o++) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+    #pragma unroll
+    for(int i = 0; i < 7 + WIN; i++)
     {
-      const float4 v = s_f[r * PW + q + WIN - 1 - j];
-      const float g = c_g[j];
-      f.x = fmaf(g, v.x, f.x); f.y = fmaf(g, v.y, f.y); f.z = fmaf(g, v.z, f.z); f.w = fmaf(g, v.w, f.w);
+      const float4 v = s_f[r * MP + q0 + i];
+      #pragma unroll
+      for(int o = 0; o < 8; o++)
+        if(o + WIN - 1 - i >= 0 && o + WIN - 1 - i < WIN) fma4(gk[o + WIN - 1 - i], v, acc[o]);
     }
-    const float2 v = s_in[(r + WIN - 1) * SW + (q + WIN - 1)];  // the centred samples at q
-    if(J.outx) J.outx[(int64_t)y * W + x] = scale * (f.x + 2.0f * v.x * f.z + v.y * f.w);
-    if(J.outy) J.outy[(int64_t)y * W + x] = scale * (f.y + 2.0f * v.y * f.z + v.x * f.w);
+    if(y >= H) continue;
+    #pragma unroll
+    for(int o = 0; o < 8; o++)
+    {
+      const int x = qx0 + q0 + o;
+      if(x >= W) break;
+      const float4 f = acc[o];
+      const float2 v = s_q[r * kBwdT + q0 + o];  // the centred samples at q
+      if(J.outx) J.outx[(int64_t)y * W + x] = scale * (f.x + 2.0f * v.x * f.z + v.y * f.w);
+      if(J.outy) J.outy[(int64_t)y * W + x] = scale * (f.y + 2.0f * v.y * f.z + v.x * f.w);
+    }
   }
 }
 
