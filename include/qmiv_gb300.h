@@ -154,6 +154,20 @@ qmiv_status qmiv_calc_frame(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic
 qmiv_status qmiv_calc_batch(qmiv_handle* h, const qmiv_job* jobs, int32_t n, qmiv_frame_result* results,
                             qmiv_stream stream);
 
+/* A batch captured once as a CUDA graph and replayed: for a fixed set of device pictures whose
+ * contents change between replays (video frames decoded into the same buffers). No
+ * counterpart in the reference. create runs the batch once, then records its launches on
+ * `stream` (a created stream, not the legacy default stream) with private copies of the job
+ * tables and TMA descriptors; launch replays them on any stream. The graph uses the handle's
+ * scratch: replays and other calls on the handle must not overlap (same stream or
+ * serialised), and the handle must outlive the graph. Results land in `results` as for
+ * qmiv_calc_batch. */
+typedef struct qmiv_graph qmiv_graph;
+qmiv_status qmiv_batch_graph_create(qmiv_handle* h, const qmiv_job* jobs, int32_t n, qmiv_frame_result* results,
+                                    qmiv_stream stream, qmiv_graph** out);
+qmiv_status qmiv_batch_graph_launch(qmiv_graph* g, qmiv_stream stream);
+qmiv_status qmiv_batch_graph_destroy(qmiv_graph* g);
+
 /* --- fine-grained calls (each synchronous; for the C++ processor shim) --------------- */
 /* xGlobClrDiffProc::CalcGlobalColorDiff(P0, P1) (xGlobClrDiff.h:41 -> xGlobClrDiff.cpp:15) */
 qmiv_status qmiv_gcd(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, int32_t gcd_r2t[4],

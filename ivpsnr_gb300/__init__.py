@@ -62,6 +62,27 @@ def make_pic(planes, bitdepth, chroma_format=CF420):
     return p
 
 
+class BatchGraph:
+    """A captured batch (qmiv_batch_graph_*): launch() replays it on a stream."""
+
+    def __init__(self, lib, g):
+        self.lib, self.g = lib, g
+
+    def launch(self, stream):
+        _abi.check(self.lib.qmiv_batch_graph_launch(self.g, stream), "qmiv_batch_graph_launch")
+
+    def close(self):
+        if self.g:
+            self.lib.qmiv_batch_graph_destroy(self.g)
+            self.g = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
 class Processor:
     """One qmiv handle: the GPU counterpart of the reference's processor objects
     (xIVPSNR / xSSIM / xIVSSIM / xGlobClrDiffProc / xShftCompPicProc)."""
@@ -121,6 +142,14 @@ class Processor:
     def calc_batch(self, jobs, results_ptr, stream=0):
         arr = (_abi.Job * len(jobs))(*jobs)
         _abi.check(self.lib.qmiv_calc_batch(self.h, arr, len(jobs), results_ptr, stream), "qmiv_calc_batch")
+
+    def capture_batch(self, jobs, results_ptr, stream):
+        """qmiv_batch_graph_create: the batch recorded once as a CUDA graph; returns a BatchGraph."""
+        arr = (_abi.Job * len(jobs))(*jobs)
+        g = ctypes.c_void_p()
+        _abi.check(self.lib.qmiv_batch_graph_create(self.h, arr, len(jobs), results_ptr, stream, ctypes.byref(g)),
+                   "qmiv_batch_graph_create")
+        return BatchGraph(self.lib, g)
 
     def finish_sequence(self):
         r = _abi.SeqResult()

@@ -70,6 +70,9 @@ SIGNATURES = [
     ("qmiv_set_options", c_i32, [_vp, _P(Options)]),
     ("qmiv_calc_frame", c_i32, [_vp, _P(Pic), _P(Pic), c_u32, _P(FrameResult), _vp]),
     ("qmiv_calc_batch", c_i32, [_vp, _P(Job), c_i32, _vp, _vp]),
+    ("qmiv_batch_graph_create", c_i32, [_vp, _P(Job), c_i32, _vp, _vp, _P(_vp)]),
+    ("qmiv_batch_graph_launch", c_i32, [_vp, _vp]),
+    ("qmiv_batch_graph_destroy", c_i32, [_vp]),
     ("qmiv_gcd", c_i32, [_vp, _P(Pic), _P(Pic), _P(c_i32), _vp]),
     ("qmiv_psnr", c_i32, [_vp, _P(Pic), _P(Pic), _P(c_f64), _P(c_f64), _vp]),
     ("qmiv_psnr_static", c_i32, [_P(Pic), _P(Pic), _P(Options), _P(FrameResult), _vp]),

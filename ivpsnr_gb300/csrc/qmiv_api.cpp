@@ -527,92 +527,112 @@ qmiv_status plan_ssim(qmiv_handle* h, const DevJob& j)
 }
 
 // Lays out the call tables of h->jobs / sjobs / steps / frames and copies them to the device.
+// Host image of the per-call tables (jobs, SSIM jobs, pyramid steps, SSIM frames), each
+// section 256-byte aligned; returns its size, or 0 if it would exceed `cap`.
+size_t pack_tables(const qmiv_handle* h, uint8_t* dst, size_t cap)
+{
+  size_t pos = 0;
+  bool ok = true;
+  auto put = [&](const void* src, size_t bytes) {
+    if(pos + bytes > cap) { ok = false; return; }
+    if(bytes) std::memcpy(dst + pos, src, bytes);
+    pos += align256(bytes);
+  };
+  put(h->jobs.data(), sizeof(DevJob) * h->jobs.size());
+  put(h->sjobs.data(), sizeof(SsimJob) * h->sjobs.size());
+  for(int s = 0; s < 4; s++) put(h->steps[s].data(), sizeof(PyrStep) * h->steps[s].size());
+  put(h->frames.data(), sizeof(SsimFrame) * h->frames.size());
+  return ok ? pos : 0;
+}
+
 qmiv_status upload_tables(qmiv_handle* h, cudaStream_t st)
 {
   CallTables& t = h->tab;
   const int k = h->tab_next;
   h->tab_next = (k + 1) % qmiv_handle::kRing;
   if(h->tab_used[k]) CUDA_TRY(cudaEventSynchronize(h->tab_ev[k]));
-  uint8_t* hb = h->h_tab[k];
-  size_t pos = 0;
-  auto put = [&](const void* src, size_t bytes) { std::memcpy(hb + pos, src, bytes); pos += align256(bytes); };
-  put(h->jobs.data(), sizeof(DevJob) * h->jobs.size());
-  put(h->sjobs.data(), sizeof(SsimJob) * h->sjobs.size());
-  for(int s = 0; s < 4; s++) put(h->steps[s].data(), sizeof(PyrStep) * h->steps[s].size());
-  put(h->frames.data(), sizeof(SsimFrame) * h->frames.size());
-  if(pos > t.bytes) return fail(QMIV_TOO_LARGE, "call tables %zu B > %zu B", pos, t.bytes);
-  CUDA_TRY(cudaMemcpyAsync(h->d_tab, hb, pos, cudaMemcpyHostToDevice, st));
+  const size_t pos = pack_tables(h, h->h_tab[k], t.bytes);
+  if(!pos) return fail(QMIV_TOO_LARGE, "call tables exceed %zu B", t.bytes);
+  CUDA_TRY(cudaMemcpyAsync(h->d_tab, h->h_tab[k], pos, cudaMemcpyHostToDevice, st));
   CUDA_TRY(cudaEventRecord(h->tab_ev[k], st));
   h->tab_used[k] = true;
   return QMIV_OK;
 }
 
-// Runs every metric of the jobs in h->jobs (each bound to its slot).
-qmiv_status run_jobs(qmiv_handle* h, cudaStream_t st)
+// The launch plan of the jobs in h->jobs: their CPS variants (sorted so that each variant's
+// jobs are contiguous), grid decomposition, tensor maps and the SSIM-family tables.
+struct LaunchPlan {
+  std::vector<int> sv;   // CPS variant per (sorted) job, -1: none
+  bool any_stats = false;
+};
+
+qmiv_status plan_jobs(qmiv_handle* h, LaunchPlan& P, cudaStream_t st)
 {
   const int n = (int)h->jobs.size();
   std::vector<int> var(n);
-  bool any_stats = false;
+  P.any_stats = false;
   for(int i = 0; i < n; i++)
   {
     DevJob& j = h->jobs[i];
     var[i] = (j.metrics & (QMIV_M_IVPSNR | QMIV_M_IVSSIM)) ? pick_cps_variant(h, j) : -1;
-    any_stats |= (j.metrics & (QMIV_M_PSNR | QMIV_M_WSPSNR | QMIV_M_IVPSNR | QMIV_M_IVSSIM)) != 0;
+    P.any_stats |= (j.metrics & (QMIV_M_PSNR | QMIV_M_WSPSNR | QMIV_M_IVPSNR | QMIV_M_IVSSIM)) != 0;
   }
-  // order jobs by CPS variant so each variant's jobs are contiguous
   std::vector<int> order(n);
   for(int i = 0; i < n; i++) order[i] = i;
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return var[a] < var[b]; });
   std::vector<DevJob> sorted(n);
-  std::vector<int> svar(n), sv(n);
-  for(int i = 0; i < n; i++) { sorted[i] = h->jobs[order[i]]; sv[i] = var[order[i]]; svar[i] = sv[i] < 0 ? 0 : sv[i]; }
+  std::vector<int> svar(n);
+  P.sv.assign(n, -1);
+  for(int i = 0; i < n; i++) { sorted[i] = h->jobs[order[i]]; P.sv[i] = var[order[i]]; svar[i] = P.sv[i] < 0 ? 0 : P.sv[i]; }
   plan_grid(h, sorted.data(), n, svar);
   int first = 0;
   while(first < n)
   {
     int last = first;
-    while(last + 1 < n && sv[last + 1] == sv[first]) last++;
+    while(last + 1 < n && P.sv[last + 1] == P.sv[first]) last++;
     int base = 0;
-    for(int i = first; i <= last; i++) { sorted[i].cps_base = base; base += sv[i] < 0 ? 0 : sorted[i].cps_strips * sorted[i].cps_segs; }
+    for(int i = first; i <= last; i++) { sorted[i].cps_base = base; base += P.sv[i] < 0 ? 0 : sorted[i].cps_strips * sorted[i].cps_segs; }
     first = last + 1;
   }
   for(int i = 0; i < n; i++)
   {
-    if(sv[i] > 0 && variants()[sv[i]].kind == 2)
+    if(P.sv[i] > 0 && variants()[P.sv[i]].kind == 2)
     {
-      qmiv_status ts = ensure_tmaps(h, sorted[i], variants()[sv[i]], st);
+      qmiv_status ts = ensure_tmaps(h, sorted[i], variants()[P.sv[i]], st);
       if(ts != QMIV_OK) return ts;
     }
   }
   h->jobs = sorted;
-  // SSIM family
   h->sjobs.clear(); h->frames.clear();
   for(int s = 0; s < 4; s++) h->steps[s].clear();
   for(int i = 0; i < n; i++)
     if(h->jobs[i].metrics & kSsimMetrics) { qmiv_status ps = plan_ssim(h, h->jobs[i]); if(ps != QMIV_OK) return ps; }
   int tb = 0;
   for(auto& s : h->sjobs) { s.tile_base = tb; tb += s.tiles_x * s.tiles_y; }
+  return QMIV_OK;
+}
 
-  qmiv_status us = upload_tables(h, st);
-  if(us != QMIV_OK) return us;
-  const CallTables& t = h->tab;
-  const DevJob* d_jobs = reinterpret_cast<const DevJob*>(h->d_tab + t.jobs_off);
+// Every launch of a plan, reading its tables from d_tab (laid out by pack_tables).
+qmiv_status launch_jobs(qmiv_handle* h, const LaunchPlan& P, const uint8_t* d_tab, cudaStream_t st)
+{
+  const int n = (int)h->jobs.size();
+  const DevJob* d_jobs = reinterpret_cast<const DevJob*>(d_tab);
   h->prof_n = 0;
-  if(any_stats)
+  if(P.any_stats)
   {
     CUDA_TRY(prof_mark(h, "k_stats", st, true));
     CUDA_TRY(launch_stats(d_jobs, h->jobs.data(), n, h->params, st));
     CUDA_TRY(prof_mark(h, "k_stats", st, false));
     h->launches++;
   }
-  first = 0;
+  int first = 0;
   while(first < n)
   {
     int last = first;
-    while(last + 1 < n && sv[last + 1] == sv[first]) last++;
-    if(sv[first] >= 0)
+    while(last + 1 < n && P.sv[last + 1] == P.sv[first]) last++;
+    if(P.sv[first] >= 0)
     {
-      const CpsVariant& cv = variants()[sv[first]];
+      const CpsVariant& cv = variants()[P.sv[first]];
       int blocks = 0;
       for(int i = first; i <= last; i++) blocks = h->jobs[i].cps_base + h->jobs[i].cps_strips * h->jobs[i].cps_segs;
       CUDA_TRY(prof_mark(h, cv.name, st, true));
@@ -624,11 +644,10 @@ qmiv_status run_jobs(qmiv_handle* h, cudaStream_t st)
   }
   if(!h->sjobs.empty())
   {
-    // the per-call layout puts the pyramid level tables after the SSIM jobs
-    size_t pos = t.jobs_off + align256(sizeof(DevJob) * n) + align256(sizeof(SsimJob) * h->sjobs.size());
+    size_t pos = align256(sizeof(DevJob) * n) + align256(sizeof(SsimJob) * h->sjobs.size());
     for(int s = 0; s < 4; s++)
     {
-      const PyrStep* d_steps = reinterpret_cast<const PyrStep*>(h->d_tab + pos);
+      const PyrStep* d_steps = reinterpret_cast<const PyrStep*>(d_tab + pos);
       if(!h->steps[s].empty())
       {
         CUDA_TRY(prof_mark(h, "k_downsample", st, true));
@@ -638,8 +657,8 @@ qmiv_status run_jobs(qmiv_handle* h, cudaStream_t st)
       }
       pos += align256(sizeof(PyrStep) * h->steps[s].size());
     }
-    const SsimFrame* d_frames = reinterpret_cast<const SsimFrame*>(h->d_tab + pos);
-    const SsimJob* d_sjobs = reinterpret_cast<const SsimJob*>(h->d_tab + t.jobs_off + align256(sizeof(DevJob) * n));
+    const SsimFrame* d_frames = reinterpret_cast<const SsimFrame*>(d_tab + pos);
+    const SsimJob* d_sjobs = reinterpret_cast<const SsimJob*>(d_tab + align256(sizeof(DevJob) * n));
     CUDA_TRY(prof_mark(h, h->opt.ssim_window == QMIV_SSIM_GAUSS11 ? "k_ssim<11>" : "k_ssim<10>", st, true));
     CUDA_TRY(launch_ssim(d_sjobs, h->sjobs.data(), (int)h->sjobs.size(), h->opt.ssim_window, st));
     CUDA_TRY(prof_mark(h, nullptr, st, false));
@@ -648,6 +667,16 @@ qmiv_status run_jobs(qmiv_handle* h, cudaStream_t st)
     h->launches++;
   }
   return QMIV_OK;
+}
+
+// Runs every metric of the jobs in h->jobs (each bound to its slot).
+qmiv_status run_jobs(qmiv_handle* h, cudaStream_t st)
+{
+  LaunchPlan P;
+  qmiv_status s = plan_jobs(h, P, st);
+  if(s != QMIV_OK) return s;
+  if((s = upload_tables(h, st)) != QMIV_OK) return s;
+  return launch_jobs(h, P, h->d_tab + h->tab.jobs_off, st);
 }
 
 // Window constants of the separable SSIM (the factor of the reference's coefficient table).
@@ -1068,13 +1097,12 @@ qmiv_status qmiv_scp(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1,
   return QMIV_OK;
 }
 
-qmiv_status qmiv_calc_batch(qmiv_handle* h, const qmiv_job* jobs, int32_t n, qmiv_frame_result* results, qmiv_stream stream)
+static qmiv_status fill_batch(qmiv_handle* h, const qmiv_job* jobs, int32_t n, qmiv_frame_result* results)
 {
   if(!h) return fail(QMIV_BAD_ARG, "handle is null");
   if(!jobs || n < 1) return fail(QMIV_BAD_ARG, "no jobs");
   if(n > h->max_jobs) return fail(QMIV_TOO_LARGE, "%d jobs > max_jobs %d", n, h->max_jobs);
   if(!results) return fail(QMIV_BAD_ARG, "results is null");
-  cudaStream_t st = (cudaStream_t)stream;
   h->jobs.assign(n, DevJob());
   for(int i = 0; i < n; i++)
   {
@@ -1096,7 +1124,96 @@ qmiv_status qmiv_calc_batch(qmiv_handle* h, const qmiv_job* jobs, int32_t n, qmi
       j.scp_stride = j.W;
     }
   }
-  return run_jobs(h, st);
+  return QMIV_OK;
+}
+
+qmiv_status qmiv_calc_batch(qmiv_handle* h, const qmiv_job* jobs, int32_t n, qmiv_frame_result* results, qmiv_stream stream)
+{
+  qmiv_status s = fill_batch(h, jobs, n, results);
+  if(s != QMIV_OK) return s;
+  return run_jobs(h, (cudaStream_t)stream);
+}
+
+// ---- a batch captured once as a CUDA graph ----------------------------------------------------
+struct qmiv_graph {
+  qmiv_handle* h = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  uint8_t* d_tab = nullptr;     // the batch's own tables
+  uint8_t* d_tmaps = nullptr;   // the batch's own tensor maps (6 per job)
+  int64_t launches = 0;         // kernels per replay
+};
+
+qmiv_status qmiv_batch_graph_destroy(qmiv_graph* g)
+{
+  if(!g) return QMIV_OK;
+  if(g->exec) cudaGraphExecDestroy(g->exec);
+  if(g->graph) cudaGraphDestroy(g->graph);
+  if(g->d_tab) cudaFree(g->d_tab);
+  if(g->d_tmaps) cudaFree(g->d_tmaps);
+  delete g;
+  return QMIV_OK;
+}
+
+qmiv_status qmiv_batch_graph_create(qmiv_handle* h, const qmiv_job* jobs, int32_t n, qmiv_frame_result* results,
+                                    qmiv_stream stream, qmiv_graph** out)
+{
+  if(!out) return fail(QMIV_BAD_ARG, "out is null");
+  *out = nullptr;
+  const cudaStream_t st = (cudaStream_t)stream;
+  if(st == nullptr) return fail(QMIV_BAD_ARG, "graph capture needs a created stream, not the legacy default stream");
+  qmiv_status s = fill_batch(h, jobs, n, results);
+  if(s != QMIV_OK) return s;
+  // one ordinary run first: validates the batch and performs every one-time set-up
+  if((s = run_jobs(h, st)) != QMIV_OK) return s;
+  CUDA_TRY(cudaStreamSynchronize(st));
+  if((s = fill_batch(h, jobs, n, results)) != QMIV_OK) return s;
+  LaunchPlan P;
+  if((s = plan_jobs(h, P, st)) != QMIV_OK) return s;
+  qmiv_graph* g = new qmiv_graph;
+  g->h = h;
+  auto bail = [&](qmiv_status e) { qmiv_batch_graph_destroy(g); return e; };
+  // private copies of the tensor maps and tables: later calls on the handle rewrite the slots'
+  if(cudaMalloc(&g->d_tmaps, (size_t)n * 6 * sizeof(CUtensorMap)) != cudaSuccess) return bail(fail(QMIV_OUT_OF_MEMORY, "graph tensor maps"));
+  for(int i = 0; i < n; i++)
+  {
+    DevJob& j = h->jobs[i];
+    if(!j.tmaps) continue;
+    uint8_t* dst = g->d_tmaps + (size_t)i * 6 * sizeof(CUtensorMap);
+    if(cudaMemcpyAsync(dst, j.tmaps, 6 * sizeof(CUtensorMap), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+      return bail(fail(QMIV_CUDA_ERROR, "graph tensor maps copy"));
+    j.tmaps = dst;
+  }
+  std::vector<uint8_t> img(h->tab.bytes);
+  const size_t bytes = pack_tables(h, img.data(), img.size());
+  if(!bytes) return bail(fail(QMIV_TOO_LARGE, "call tables exceed %zu B", h->tab.bytes));
+  if(cudaMalloc(&g->d_tab, bytes) != cudaSuccess) return bail(fail(QMIV_OUT_OF_MEMORY, "graph tables"));
+  if(cudaMemcpyAsync(g->d_tab, img.data(), bytes, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+     cudaStreamSynchronize(st) != cudaSuccess)
+    return bail(fail(QMIV_CUDA_ERROR, "graph tables copy"));
+  const bool prof = h->profiling;
+  h->profiling = false;
+  const int64_t l0 = h->launches;
+  if(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+  { h->profiling = prof; return bail(fail(QMIV_CUDA_ERROR, "cudaStreamBeginCapture")); }
+  s = launch_jobs(h, P, g->d_tab, st);
+  const cudaError_t ce = cudaStreamEndCapture(st, &g->graph);
+  h->profiling = prof;
+  g->launches = h->launches - l0;
+  h->launches = l0;
+  if(s != QMIV_OK) return bail(s);
+  if(ce != cudaSuccess) return bail(fail(QMIV_CUDA_ERROR, "cudaStreamEndCapture: %s", cudaGetErrorString(ce)));
+  if(cudaGraphInstantiate(&g->exec, g->graph, 0) != cudaSuccess) return bail(fail(QMIV_CUDA_ERROR, "cudaGraphInstantiate"));
+  *out = g;
+  return QMIV_OK;
+}
+
+qmiv_status qmiv_batch_graph_launch(qmiv_graph* g, qmiv_stream stream)
+{
+  if(!g || !g->exec) return fail(QMIV_BAD_ARG, "graph is null");
+  CUDA_TRY(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
+  g->h->launches += g->launches;
+  return QMIV_OK;
 }
 
 qmiv_status qmiv_ssim(qmiv_handle* h, const qmiv_pic* tst, const qmiv_pic* ref, int32_t calc_l, double ssim[4], qmiv_stream stream)
