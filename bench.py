@@ -365,6 +365,10 @@ def run_ours(args):
         if world > 1:
             dist.barrier()
 
+    # ---- CPS variant picked by the autotuner on this batch (qmiv_autotune_cps) ----
+    tuned = P.autotune_cps(qjobs, res_dev.data_ptr(), 2, sptr)
+    autotune = {"variant": tuned[1], "cps_ms": tuned[2]}
+
     # ---- device-resident batched throughput ----
     for _ in range(args.warmup):
         P.calc_batch(qjobs, res_dev.data_ptr(), sptr)
@@ -429,6 +433,28 @@ def run_ours(args):
     alg_ops = px_per_step * 2 * (25 * 9 + 10)
     sm_mhz = clk.get("sm_mhz") or 1900.0
     int_peak = 152 * 128 * sm_mhz * 1e6  # INT32 lanes x clock (derived from the sampled clock)
+
+    # ---- the same batch captured once as a CUDA graph and replayed (qmiv_batch_graph_*) ----
+    graph_line = None
+    try:
+        gstream = torch.cuda.Stream(dev)
+        gsp = gstream.cuda_stream
+        with torch.cuda.stream(gstream):
+            G = P.capture_batch(qjobs, res_dev.data_ptr(), gsp)
+            for _ in range(args.warmup):
+                G.launch(gsp)
+            gstream.synchronize()
+            ge0, ge1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ge0.record(gstream)
+            for _ in range(args.steps):
+                G.launch(gsp)
+            ge1.record(gstream)
+            gstream.synchronize()
+            graph_ms = ge0.elapsed_time(ge1) / args.steps
+            G.close()
+        graph_line = {"ms_per_step": graph_ms, "value": px_per_step / (graph_ms * 1e-3) / 1e9, "unit": "Gpixel/s"}
+    except Exception as ex:
+        graph_line = {"unavailable": str(ex)[:200]}
 
     # ---- plain per-frame form: one qmiv_calc_frame per pair (device inputs) ----
     Pp = q.Processor(4096, 2048, max_jobs=1, scratch_metrics=PSNRS)
@@ -498,6 +524,8 @@ def run_ours(args):
                              "peak_kind": "152 SMs x 128 INT32 lanes x sampled SM clock"},
             "kernel_ms": kavg,
             "plain": {"value": plain_value, "unit": "Gpixel/s", "batched_over_plain": value / world / plain_value},
+            "graph": graph_line,
+            "autotune": autotune,
             "check": {"ivpsnr_pair0": r0.ivpsnr, "gcd_pair0": list(r0.gcd_r2t)[:3]},
         }
         if ssim_line:

@@ -253,6 +253,12 @@ int64_t     qmiv_kernel_launches(const qmiv_handle* h);
 int32_t     qmiv_cps_variant_count(void);
 const char* qmiv_cps_variant_name(int32_t v);
 qmiv_status qmiv_set_cps_variant(qmiv_handle* h, int32_t v);
+/* Autotuner: times every compiled CPS variant that fits all IV-PSNR / IV-SSIM jobs of the batch
+ * (reps timed runs each after one warm-up, CUDA events around the CPS launches) and keeps the
+ * fastest as the handle's override. Runs the batch as qmiv_calc_batch does (results are
+ * written). best_variant / best_ms (may be null) receive the choice and its CPS time. */
+qmiv_status qmiv_autotune_cps(qmiv_handle* h, const qmiv_job* jobs, int32_t n, qmiv_frame_result* results,
+                              int32_t reps, qmiv_stream stream, int32_t* best_variant, double* best_ms);
 /* Per-kernel timing of the most recent calc call (CUDA events recorded on the call's
  * stream around each launch, when enabled). qmiv_kernel_times synchronises with those
  * events and returns up to max launches: names[i] (static strings) and ms[i]. */

@@ -159,6 +159,15 @@ class Processor:
     def set_cps_variant(self, v):
         _abi.check(self.lib.qmiv_set_cps_variant(self.h, v), "qmiv_set_cps_variant")
 
+    def autotune_cps(self, jobs, results_ptr, reps=3, stream=0):
+        """qmiv_autotune_cps: (variant index, variant name, CPS ms) of the fastest fitting variant,
+        which the handle keeps using."""
+        arr = (_abi.Job * len(jobs))(*jobs)
+        best, ms = ctypes.c_int32(), ctypes.c_double()
+        _abi.check(self.lib.qmiv_autotune_cps(self.h, arr, len(jobs), results_ptr, reps, stream, ctypes.byref(best),
+                                              ctypes.byref(ms)), "qmiv_autotune_cps")
+        return best.value, self.lib.qmiv_cps_variant_name(best.value).decode(), ms.value
+
     def set_profiling(self, on=True):
         _abi.check(self.lib.qmiv_set_profiling(self.h, int(on)), "qmiv_set_profiling")
 

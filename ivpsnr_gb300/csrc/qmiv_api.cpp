@@ -205,27 +205,31 @@ bool tma_ok(const DevJob& j)
   return true;
 }
 
+// Can compiled variant v run job j? (its search range, key width, staging kind and sample size)
+bool cps_variant_fits(const qmiv_handle* h, const DevJob& j, int v)
+{
+  const auto& V = variants();
+  if(v <= 0 || v >= (int)V.size()) return false;
+  const int sr = h->params.sr;
+  if(!j.cshift || h->opt.cmp_w_search[0] < 1 || sr < 1 || sr > 4) return false;
+  const CpsVariant& c = V[v];
+  if(c.sr != sr || c.key64 != !key32_ok(h, j.bd)) return false;
+  if(c.kind == 2 && (!tma_ok(j) || c.sbytes != j.sbytes)) return false;
+  return c.kind != 0;
+}
+
 int pick_cps_variant(const qmiv_handle* h, const DevJob& j)
 {
   const auto& V = variants();
   const int sr = h->params.sr;
   if(!j.cshift || h->opt.cmp_w_search[0] < 1 || sr < 1 || sr > 4) return 0; // generic
   if(h->cps_variant_override == 0) return 0;
-  const bool k64 = !key32_ok(h, j.bd);
-  const bool tma = tma_ok(j);
-  auto fits = [&](int v) {
-    const CpsVariant& c = V[v];
-    if(c.sr != sr || c.key64 != k64) return false;
-    if(c.kind == 2 && (!tma || c.sbytes != j.sbytes)) return false;
-    return c.kind != 0;
-  };
-  if(h->cps_variant_override > 0 && h->cps_variant_override < (int)V.size() && fits(h->cps_variant_override))
-    return h->cps_variant_override;
+  if(cps_variant_fits(h, j, h->cps_variant_override)) return h->cps_variant_override;
   // default: the TMA kernel with 32-row strips and 8 warps, else the staged-load kernel
   for(int v = 1; v < (int)V.size(); v++)
-    if(fits(v) && V[v].kind == 2 && V[v].rows == 32 && std::strstr(V[v].name, "_q4_w4")) return v;
+    if(cps_variant_fits(h, j, v) && V[v].kind == 2 && V[v].rows == 32 && std::strstr(V[v].name, "_q4_w4")) return v;
   for(int v = 1; v < (int)V.size(); v++)
-    if(fits(v) && V[v].kind == 1 && std::strstr(V[v].name, "rpt8_nwg2")) return v;
+    if(cps_variant_fits(h, j, v) && V[v].kind == 1 && std::strstr(V[v].name, "rpt8_nwg2")) return v;
   return 0;
 }
 
@@ -1213,6 +1217,59 @@ qmiv_status qmiv_batch_graph_launch(qmiv_graph* g, qmiv_stream stream)
   if(!g || !g->exec) return fail(QMIV_BAD_ARG, "graph is null");
   CUDA_TRY(cudaGraphLaunch(g->exec, (cudaStream_t)stream));
   g->h->launches += g->launches;
+  return QMIV_OK;
+}
+
+// ---- CPS variant autotuner ---------------------------------------------------------------
+qmiv_status qmiv_autotune_cps(qmiv_handle* h, const qmiv_job* jobs, int32_t n, qmiv_frame_result* results,
+                              int32_t reps, qmiv_stream stream, int32_t* best_variant, double* best_ms)
+{
+  if(!h) return fail(QMIV_BAD_ARG, "handle is null");
+  const cudaStream_t st = (cudaStream_t)stream;
+  if(reps < 1) reps = 3;
+  qmiv_status s = fill_batch(h, jobs, n, results);
+  if(s != QMIV_OK) return s;
+  std::vector<int> cand;
+  for(int v = 1; v < (int)variants().size(); v++)
+  {
+    bool all = true, any = false;
+    for(const DevJob& j : h->jobs)
+    {
+      if(!(j.metrics & (QMIV_M_IVPSNR | QMIV_M_IVSSIM))) continue;
+      any = true;
+      all = all && cps_variant_fits(h, j, v);
+    }
+    if(any && all) cand.push_back(v);
+  }
+  const int saved = h->cps_variant_override;
+  const bool prof = h->profiling;
+  if(!prof) { s = (qmiv_status)qmiv_set_profiling(h, 1); if(s != QMIV_OK) return s; }
+  int best = saved;
+  double best_t = 1e300;
+  for(int v : cand)
+  {
+    h->cps_variant_override = v;
+    double tmin = 1e300;
+    for(int r = 0; r < reps + 1; r++)  // the first run of a variant is a warm-up
+    {
+      if((s = fill_batch(h, jobs, n, results)) != QMIV_OK || (s = run_jobs(h, st)) != QMIV_OK) break;
+      const char* names[64];
+      double ms[64];
+      const int k = qmiv_kernel_times(h, names, ms, 64);
+      double t = 0;
+      for(int i = 0; i < k; i++)
+        if(names[i] && std::strcmp(names[i], "k_stats") && std::strcmp(names[i], "k_downsample") && std::strncmp(names[i], "k_ssim", 6))
+          t += ms[i];
+      if(r > 0 && t < tmin) tmin = t;
+    }
+    if(s != QMIV_OK) break;
+    if(tmin < best_t) { best_t = tmin; best = v; }
+  }
+  if(!prof) qmiv_set_profiling(h, 0);
+  if(s != QMIV_OK) { h->cps_variant_override = saved; return s; }
+  h->cps_variant_override = cand.empty() ? saved : best;
+  if(best_variant) *best_variant = h->cps_variant_override;
+  if(best_ms) *best_ms = cand.empty() ? 0.0 : best_t;
   return QMIV_OK;
 }
 

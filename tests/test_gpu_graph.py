@@ -86,3 +86,29 @@ def test_graph_rejects_default_stream(gpu_lib):
     with gpu_lib.Processor(64, 32) as P:
         with pytest.raises(gpu_lib.QmivError):
             P.capture_batch([j], res.data_ptr(), 0)
+
+
+def test_autotuner_picks_a_fitting_variant_and_keeps_results(gpu_lib):
+    import torch
+    from ivpsnr_gb300 import _abi
+    jobs, keep = [], []
+    for i, (w, h) in enumerate([(1920, 1080), (1280, 720)]):
+        d0, d1 = _device_pair(w, h, 10, 600 + i, True)
+        keep.append((d0, d1))
+        j = _abi.Job()
+        j.pic0 = gpu_lib.make_pic(d0, 10)
+        j.pic1 = gpu_lib.make_pic(d1, 10)
+        j.metrics = gpu_lib.M_PSNR | gpu_lib.M_IVPSNR
+        jobs.append(j)
+    rs = ctypes.sizeof(_abi.FrameResult)
+    res = torch.zeros(len(jobs) * rs, dtype=torch.uint8, device="cuda")
+    with gpu_lib.Processor(1920, 1080, max_jobs=2) as P:
+        P.calc_batch(jobs, res.data_ptr())
+        torch.cuda.synchronize()
+        want = _results(res, 2)
+        v, name, ms = P.autotune_cps(jobs, res.data_ptr(), reps=2)
+        assert v > 0 and name.startswith(("tma420_sr2", "cps420_sr2")) and ms > 0
+        res.zero_()
+        P.calc_batch(jobs, res.data_ptr())
+        torch.cuda.synchronize()
+        assert _results(res, 2) == want
