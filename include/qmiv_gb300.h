@@ -147,6 +147,23 @@ qmiv_status qmiv_set_options(qmiv_handle* h, const qmiv_options* opt);
 qmiv_status qmiv_calc_frame(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, uint32_t metrics,
                             qmiv_frame_result* out, qmiv_stream stream);
 
+/* Masked form: xPSNR::calcPicPSNRM (xPSNR.cpp:42), xWSPSNR::calcPicWSPSNRM (xWSPSNR.cpp:61),
+ * xIVPSNRM::calcPicIVPSNRM (xIVPSNR.cpp:138-200) and xGlobClrDiff::CalcGlobalColorDiffM
+ * (xGlobClrDiff.cpp:52-83), as the application runs them with -im (xAppQMIV.cpp:693-695,
+ * 831-893). The mask is one luma-resolution plane (width x height of the pictures, its own bit
+ * depth) weighting all three components; mask 0 excludes a pixel as a tested pixel and as a
+ * search candidate. metrics: any of QMIV_M_PSNR, QMIV_M_WSPSNR, QMIV_M_IVPSNR; gcd_r2t holds the
+ * masked GCD. Synchronous; the frame is added to the sequence statistics. */
+typedef struct qmiv_mask {
+  const void* plane;
+  int32_t     stride;       /* in samples */
+  int32_t     bitdepth;     /* the mask's peak is 2^bitdepth - 1 */
+  int32_t     sample_bytes; /* 1 or 2 */
+  int32_t     is_device;
+} qmiv_mask;
+qmiv_status qmiv_calc_frame_masked(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, const qmiv_mask* mask,
+                                   uint32_t metrics, qmiv_frame_result* out, qmiv_stream stream);
+
 /* Batched form: n jobs of mixed sizes in one launch sequence on `stream`, asynchronous.
  * results (n entries) must be device memory or host memory the device can write
  * (cudaHostAlloc'd); they are valid after the stream synchronises. Frames are not added

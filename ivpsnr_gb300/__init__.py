@@ -118,6 +118,15 @@ class Processor:
                                             ctypes.byref(r), stream), "qmiv_calc_frame")
         return r.to_dict()
 
+    def calc_frame_masked(self, pic0, pic1, mask, mask_bitdepth=8, metrics=M_PSNR | M_WSPSNR | M_IVPSNR, stream=0):
+        """qmiv_calc_frame_masked; mask: a 2-D uint8/uint16 numpy array or torch tensor (luma size)."""
+        addr, stride, is_dev, isz = _ptr_and_stride(mask)
+        m = _abi.Mask(addr, stride, mask_bitdepth, isz, is_dev)
+        r = _abi.FrameResult()
+        _abi.check(self.lib.qmiv_calc_frame_masked(self.h, ctypes.byref(pic0), ctypes.byref(pic1), ctypes.byref(m),
+                                                   metrics, ctypes.byref(r), stream), "qmiv_calc_frame_masked")
+        return r.to_dict()
+
     def gcd(self, pic0, pic1, stream=0):
         g = (ctypes.c_int32 * 4)()
         _abi.check(self.lib.qmiv_gcd(self.h, ctypes.byref(pic0), ctypes.byref(pic1), g, stream), "qmiv_gcd")

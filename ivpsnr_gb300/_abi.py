@@ -52,6 +52,11 @@ class SeqResult(ctypes.Structure):
                 ("ssim_pic", c_f64), ("msssim", c_f64 * 4), ("msssim_pic", c_f64), ("ivssim", c_f64)]
 
 
+class Mask(ctypes.Structure):
+    _fields_ = [("plane", ctypes.c_void_p), ("stride", c_i32), ("bitdepth", c_i32), ("sample_bytes", c_i32),
+                ("is_device", c_i32)]
+
+
 class Job(ctypes.Structure):
     _fields_ = [("pic0", Pic), ("pic1", Pic), ("metrics", c_u32), ("use_ws", c_i32),
                 ("scp0", ctypes.c_void_p * 3), ("scp1", ctypes.c_void_p * 3), ("scp_stride", c_i32)]
@@ -69,6 +74,7 @@ SIGNATURES = [
     ("qmiv_destroy", c_i32, [_vp]),
     ("qmiv_set_options", c_i32, [_vp, _P(Options)]),
     ("qmiv_calc_frame", c_i32, [_vp, _P(Pic), _P(Pic), c_u32, _P(FrameResult), _vp]),
+    ("qmiv_calc_frame_masked", c_i32, [_vp, _P(Pic), _P(Pic), _P(Mask), c_u32, _P(FrameResult), _vp]),
     ("qmiv_calc_batch", c_i32, [_vp, _P(Job), c_i32, _vp, _vp]),
     ("qmiv_batch_graph_create", c_i32, [_vp, _P(Job), c_i32, _vp, _vp, _P(_vp)]),
     ("qmiv_batch_graph_launch", c_i32, [_vp, _vp]),

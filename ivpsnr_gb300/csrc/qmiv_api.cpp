@@ -17,6 +17,7 @@
 
 #include "qmiv_internal.h"
 #include "qmiv_loss.h"
+#include "qmiv_masked.h"
 #include "qmiv_ssim.h"
 
 using namespace qmiv;
@@ -128,6 +129,10 @@ struct qmiv_handle {
   std::vector<SsimFrame> frames;
   // staging for host pictures (2 pictures, planar, up to uint16 4:4:4)
   uint16_t* d_stage[2] = { nullptr, nullptr };
+  // masked frames: per-row sums, counters / count / GCD, host-mask staging
+  int64_t* mask_rows = nullptr;
+  uint8_t* mask_small = nullptr;
+  uint16_t* mask_stage = nullptr;
   std::map<std::pair<int, int>, std::pair<double*, double>> ws_cache;
   SeqAcc seq;
   int64_t launches = 0;
@@ -849,6 +854,10 @@ qmiv_status qmiv_create(qmiv_handle** out, const qmiv_options* opt, int32_t max_
     const size_t e = (size_t)((max_w + 7) & ~7) * max_h * 3 + 64;
     if(cudaMalloc(&h->d_stage[i], e * sizeof(uint16_t)) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "staging"));
   }
+  if(cudaMalloc(&h->mask_rows, sizeof(int64_t) * kMaskRowVals * max_h) != cudaSuccess ||
+     cudaMalloc(&h->mask_small, 256) != cudaSuccess || cudaMemset(h->mask_small, 0, 256) != cudaSuccess ||
+     cudaMalloc(&h->mask_stage, sizeof(uint16_t) * (size_t)max_w * max_h) != cudaSuccess)
+    return cleanup(fail(QMIV_OUT_OF_MEMORY, "mask scratch"));
   if(cudaDeviceSynchronize() != cudaSuccess) return cleanup(fail(QMIV_CUDA_ERROR, "create sync"));
   *out = h;
   return QMIV_OK;
@@ -864,6 +873,9 @@ qmiv_status qmiv_destroy(qmiv_handle* h)
   cudaFree(h->d_tab);
   for(int k = 0; k < qmiv_handle::kRing; k++) { cudaFreeHost(h->h_tab[k]); if(h->tab_ev[k]) cudaEventDestroy(h->tab_ev[k]); }
   for(int i = 0; i < 2; i++) cudaFree(h->d_stage[i]);
+  cudaFree(h->mask_rows);
+  cudaFree(h->mask_small);
+  cudaFree(h->mask_stage);
   for(auto& kv : h->ws_cache) cudaFree(kv.second.first);
   for(auto& p : h->prof) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
   delete h;
@@ -968,6 +980,63 @@ qmiv_status qmiv_calc_frame(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic
   if(!out) return fail(QMIV_BAD_ARG, "out is null");
   qmiv_status s = frame_common(h, pic0, pic1, metrics, nullptr, nullptr, nullptr, 0, out, (cudaStream_t)stream);
   if(s != QMIV_OK) return s;
+  seq_add(h, metrics, out);
+  return QMIV_OK;
+}
+
+qmiv_status qmiv_calc_frame_masked(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, const qmiv_mask* mask,
+                                   uint32_t metrics, qmiv_frame_result* out, qmiv_stream stream)
+{
+  if(!h || !out) return fail(QMIV_BAD_ARG, "handle or out is null");
+  const cudaStream_t st = (cudaStream_t)stream;
+  qmiv_status s = check_pair(h, pic0, pic1);
+  if(s != QMIV_OK) return s;
+  if(metrics & ~(QMIV_M_PSNR | QMIV_M_WSPSNR | QMIV_M_IVPSNR))
+    return fail(QMIV_UNSUPPORTED, "masked metrics are PSNR, WS-PSNR and IV-PSNR (requested 0x%x)", metrics);
+  if(!mask || !mask->plane) return fail(QMIV_BAD_ARG, "mask is null");
+  if(mask->sample_bytes != 1 && mask->sample_bytes != 2) return fail(QMIV_BAD_ARG, "mask sample_bytes %d", mask->sample_bytes);
+  if(mask->bitdepth < 1 || mask->bitdepth > 8 * mask->sample_bytes) return fail(QMIV_BAD_ARG, "mask bit depth %d", mask->bitdepth);
+  if(mask->stride < pic0->width) return fail(QMIV_BAD_ARG, "mask stride %d < width %d", mask->stride, pic0->width);
+  qmiv_pic a, b;
+  if((s = upload_pic(h, pic0, 0, &a, st)) != QMIV_OK) return s;
+  if((s = upload_pic(h, pic1, 1, &b, st)) != QMIV_OK) return s;
+  MaskJob j;
+  std::memset(&j, 0, sizeof(j));
+  for(int c = 0; c < 3; c++) { j.p0[c] = a.plane[c]; j.p1[c] = b.plane[c]; j.s0[c] = a.stride[c]; j.s1[c] = b.stride[c]; }
+  j.W = a.width; j.H = a.height; j.bd = a.bitdepth; j.sbytes = a.sample_bytes;
+  j.cshift = a.chroma_format == QMIV_CF420 ? 1 : 0;
+  if(mask->is_device) { j.mask = mask->plane; j.mstride = mask->stride; }
+  else
+  {
+    CUDA_TRY(cudaMemcpy2DAsync(h->mask_stage, (size_t)j.W * mask->sample_bytes, mask->plane,
+                               (size_t)mask->stride * mask->sample_bytes, (size_t)j.W * mask->sample_bytes, j.H,
+                               cudaMemcpyHostToDevice, st));
+    j.mask = h->mask_stage; j.mstride = j.W;
+  }
+  j.msbytes = mask->sample_bytes; j.mbd = mask->bitdepth;
+  j.metrics = metrics;
+  j.use_ws = h->opt.use_ws;
+  if(j.use_ws) { if((s = ws_weights(h, j.H, &j.ws, &j.ws_corr)) != QMIV_OK) return s; }
+  j.fake_exact = h->opt.fake_exact;
+  j.sr = h->opt.search_range;
+  for(int c = 0; c < 3; c++)
+  {
+    j.w_search[c] = h->opt.cmp_w_search[c]; j.w_avg[c] = h->opt.cmp_w_avg[c];
+    j.maxdiff[c] = h->params.maxdiff_for_bd[j.bd][c];
+  }
+  j.counters = reinterpret_cast<uint32_t*>(h->mask_small);
+  j.nnm = reinterpret_cast<long long*>(h->mask_small + 16);
+  j.gcd = reinterpret_cast<int32_t*>(h->mask_small + 32);
+  j.rows = h->mask_rows;
+  j.cps_rows = h->slots[0].cps_rows;
+  j.result = h->d_results;
+  CUDA_TRY(cudaMemsetAsync(h->d_results, 0, sizeof(qmiv_frame_result), st));
+  CUDA_TRY(launch_masked(j, st));
+  h->launches += (metrics & QMIV_M_IVPSNR) ? 2 : 1;
+  CUDA_TRY(cudaMemcpyAsync(h->h_results, h->d_results, sizeof(qmiv_frame_result), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  *out = h->h_results[0];
+  out->metrics = metrics;
   seq_add(h, metrics, out);
   return QMIV_OK;
 }

@@ -45,6 +45,58 @@ CASES = [
 ]
 
 
+# masked cases (-im): name, w, h, bd, seed, generator kwargs, harness options, mask kind
+MASKED_CASES = [
+    ("masked_8bit_ellipses_160x96", 160, 96, 8, 301, {}, {}, "ellipses"),
+    ("masked_10bit_graded_128x64", 128, 64, 10, 302, {"holes": True}, {}, "graded"),
+    ("masked_10bit_erp_ellipses_256x128", 256, 128, 10, 303, {}, {"erp": True}, "ellipses"),
+    ("masked_10bit_sr3_graded_96x64", 96, 64, 10, 304, {}, {"sr": 3}, "graded"),
+    ("masked_8bit_cfg0_1920x1080", 1920, 1080, 8, synth.seed_for(0, 0, 0), {}, {}, "ellipses"),
+]
+
+
+def make_mask(w, h, seed, kind):
+    """Deterministic 8-bit mask: 'ellipses' (0 inside a few ellipses, 255 elsewhere) or 'graded'
+    (values 0..255 from a smooth ramp with a zero band)."""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:h, 0:w].astype(np.float64)
+    if kind == "ellipses":
+        m = np.full((h, w), 255, np.uint16)
+        for _ in range(4):
+            cx, cy = rng.uniform(0, w), rng.uniform(0, h)
+            ax, ay = rng.uniform(0.05, 0.25) * w, rng.uniform(0.05, 0.25) * h
+            m[((x - cx) / ax) ** 2 + ((y - cy) / ay) ** 2 <= 1.0] = 0
+        return m
+    m = np.clip(np.round(255.0 * (0.5 + 0.5 * np.sin(x / (w / 3.0) + y / (h / 2.0)))), 0, 255).astype(np.uint16)
+    m[:, w // 3:w // 3 + max(1, w // 10)] = 0
+    return m
+
+
+def run_masked_case(name, w, h, bd, seed, gkw, hopt, kind, tmp):
+    ref, tst = synth.pair420(w, h, bd, seed=seed, **gkw)
+    a, b, mk = os.path.join(tmp, "a.yuv"), os.path.join(tmp, "b.yuv"), os.path.join(tmp, "m.yuv")
+    if bd == 8:
+        ref.astype(np.uint8).tofile(a)
+        tst.astype(np.uint8).tofile(b)
+    else:
+        ref.tofile(a)
+        tst.tofile(b)
+    mask = make_mask(w, h, seed, kind)
+    np.concatenate([mask.astype(np.uint8).ravel(), np.zeros(2 * (w // 2) * (h // 2), np.uint8)]).tofile(mk)
+    cmd = [HARNESS, "-w", str(w), "-h", str(h), "-bd", str(bd), "-cf", "420", "-i0", a, "-i1", b, "-nth", "2",
+           "-im", mk, "-bdm", "8"]
+    if hopt.get("erp"):
+        cmd += ["-erp", "-lat", str(hopt.get("lat", 180))]
+    if "sr" in hopt:
+        cmd += ["-sr", str(hopt["sr"])]
+    out = json.loads(subprocess.check_output(cmd).decode().splitlines()[0])
+    out.pop("frame", None)
+    return {
+        "name": name, "w": w, "h": h, "bd": bd, "seed": seed, "gen": {k: list(v) if isinstance(v, tuple) else v for k, v in gkw.items()},
+        "opts": hopt, "mask": kind, "mask_bd": 8, "input_md5": md5(ref, tst), "mask_md5": md5(mask), "expected": out,
+    }
+
+
 def md5(*arrays):
     h = hashlib.md5()
     for a in arrays:
@@ -89,6 +141,12 @@ def main():
         json.dump({"generator": "ivpsnr_gb300.synth.pair420", "reference": "pmbb-ivqm via oracle/ref_harness.cpp",
                    "cases": cases}, f, indent=1)
     print("wrote", path, len(cases), "cases")
+    masked = [run_masked_case(*c, tmp) for c in MASKED_CASES]
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "masked.json")
+    with open(path, "w") as f:
+        json.dump({"generator": "ivpsnr_gb300.synth.pair420 + make_golden.make_mask",
+                   "reference": "pmbb-ivqm via oracle/ref_harness.cpp -im", "cases": masked}, f, indent=1)
+    print("wrote", path, len(masked), "masked cases")
 
 
 if __name__ == "__main__":

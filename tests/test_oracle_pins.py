@@ -192,3 +192,27 @@ def test_ws_weights_match_closed_form(oq):
     w, corr = oq.ws_weights(h, 180)
     np.testing.assert_allclose(w, np.cos((np.arange(h) + 0.5 - h / 2) * np.pi / h), atol=1e-15)
     assert abs(corr - h / w.sum()) < 1e-12
+
+
+# ---- masked golden cases (reference harness with -im) ---------------------------------------
+MASKED = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "masked.json")))
+
+
+@pytest.mark.parametrize("case", MASKED["cases"], ids=[c["name"] for c in MASKED["cases"]])
+def test_oracle_matches_masked_golden(oq, case):
+    from tests.golden.make_golden import make_mask
+    w, h, bd = case["w"], case["h"], case["bd"]
+    gen = dict(case["gen"])
+    ref, tst = synth.pair420(w, h, bd, seed=case["seed"], **gen)
+    mask = make_mask(w, h, case["seed"], case["mask"])
+    p0 = oq.upsample420(synth.split420(ref, w, h), w, h)
+    p1 = oq.upsample420(synth.split420(tst, w, h), w, h)
+    o = case["opts"]
+    r = oq.masked(p0, p1, mask, bd, mask_bd=case["mask_bd"], use_ws=o.get("erp", False),
+                  lat_range_deg=o.get("lat", 180), search_range=o.get("sr", 2), nthreads=8)
+    e = case["expected"]
+    assert r["nnm"] == e["nnm"] and r["gcd"] == e["gcd"]
+    np.testing.assert_allclose(r["psnr"], e["psnr"], rtol=0, atol=DB_TOL)
+    np.testing.assert_allclose(r["wspsnr"], e["wspsnr"], rtol=0, atol=DB_TOL)
+    for k in ("ivpsnr", "ivpsnr_r2t", "ivpsnr_t2r"):
+        assert abs(r[k] - e[k]) <= DB_TOL, k
