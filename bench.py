@@ -240,6 +240,89 @@ def ssim_workload(args, dev, stream):
             "check": {"ivssim_frame0": r0.ivssim, "ssim_frame0": list(r0.ssim)[:3]}}
 
 
+STREAM_WORKLOAD = ("erp-8k-sequence-stream: 120 frames 7680x3840 ERP 10-bit 4:2:0 from pinned host memory, "
+                   "IV-PSNR SR 4 + WS-PSNR + IV-SSIM + MS-SSIM per frame, uploads overlapped with compute")
+
+
+def stream_workload(args, dev):
+    """Config 4: a long 8K ERP sequence streamed from pinned host memory. A copy stream uploads
+    frame i+1 into one of two device buffer pairs while the compute stream measures frame i
+    (qmiv_calc_batch, one pair per call); events order the two. Eight distinct frames are
+    generated and cycled (the content does not change the work). Reported: whole-sequence
+    Gpixel/s including every upload, next to the device-resident time per frame."""
+    import ctypes as C
+
+    import torch
+
+    import ivpsnr_gb300 as q
+    from ivpsnr_gb300 import _abi, synth
+    w, h, nf, uniq = 7680, 3840, 120, 8
+    n = w * h + 2 * (w // 2) * (h // 2)
+    host = []
+    for f in range(uniq):
+        r = torch.empty(n, dtype=torch.int16, pin_memory=True)
+        t = torch.empty(n, dtype=torch.int16, pin_memory=True)
+        synth.pair420(w, h, BD, seed=synth.seed_for(4, 0, f), holes=True,
+                      out=(r.numpy().view(np.uint16), t.numpy().view(np.uint16)))
+        host.append((r, t))
+    slots = [(torch.empty(n, dtype=torch.int16, device=dev), torch.empty(n, dtype=torch.int16, device=dev)) for _ in range(2)]
+    a, ca = w * h, (w // 2) * (h // 2)
+    pl = lambda t: [t[:a].view(h, w), t[a:a + ca].view(h // 2, w // 2), t[a + ca:].view(h // 2, w // 2)]
+    metrics = q.M_PSNR | q.M_WSPSNR | q.M_IVPSNR | q.M_MSSSIM | q.M_IVSSIM
+    jobs = []
+    for d0, d1 in slots:
+        j = _abi.Job()
+        j.pic0 = q.make_pic(pl(d0), BD)
+        j.pic1 = q.make_pic(pl(d1), BD)
+        j.pic0.sample_bytes = j.pic1.sample_bytes = 2
+        j.metrics = metrics
+        j.use_ws = 1
+        jobs.append(j)
+    rsz = C.sizeof(_abi.FrameResult)
+    res = torch.zeros(nf * rsz, dtype=torch.uint8, device=dev)
+    P = q.Processor(w, h, max_jobs=1, search_range=4, use_ws=True, scratch_metrics=metrics)
+    cs, ks = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    copied = [torch.cuda.Event() for _ in range(2)]
+    done = [torch.cuda.Event() for _ in range(2)]
+
+    def run(frames):
+        for i in range(frames):
+            s = i % 2
+            src = host[i % uniq]
+            with torch.cuda.stream(cs):
+                cs.wait_event(done[s])
+                slots[s][0].copy_(src[0], non_blocking=True)
+                slots[s][1].copy_(src[1], non_blocking=True)
+                copied[s].record(cs)
+            ks.wait_event(copied[s])
+            P.calc_batch([jobs[s]], res.data_ptr() + (i % nf) * rsz, ks.cuda_stream)
+            done[s].record(ks)
+
+    run(4)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    run(nf)
+    torch.cuda.synchronize()
+    secs = time.perf_counter() - t0
+    # device-resident: the same calls without uploads
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ks)
+    for i in range(8):
+        P.calc_batch([jobs[i % 2]], res.data_ptr(), ks.cuda_stream)
+    e1.record(ks)
+    torch.cuda.synchronize()
+    dev_ms = e0.elapsed_time(e1) / 8
+    r0 = _abi.FrameResult.from_buffer_copy(bytes(res[:rsz].cpu().numpy()))
+    P.close()
+    del slots, host
+    torch.cuda.empty_cache()
+    return {"workload": STREAM_WORKLOAD, "value": nf * w * h / secs / 1e9, "unit": "Gpixel/s (with uploads)",
+            "seconds": secs, "ms_per_frame": secs * 1e3 / nf, "device_ms_per_frame": dev_ms,
+            "h2d_bytes_per_frame": 2 * n * 2,
+            "check": {"ivpsnr_frame0": r0.ivpsnr, "wspsnr_frame0": list(r0.wspsnr)[:3], "ivssim_frame0": r0.ivssim,
+                      "msssim_frame0": list(r0.msssim)[:3]}}
+
+
 LOSS_WORKLOAD = ("ivssim-ivpsnr-loss-fwd-bwd: 16 x FP32 4:4:4 1024x1024 in [0,1], tested = reference + N(0, 0.02^2)"
                  " + per-channel offset + block shifts, SR 2, REF10 window")
 
@@ -327,6 +410,11 @@ def run_ours(args):
         return
     if args.workload == "loss":
         r = loss_workload(args, dev)
+        if rank == 0:
+            print(json.dumps(r))
+        return
+    if args.workload == "stream":
+        r = stream_workload(args, dev)
         if rank == 0:
             print(json.dumps(r))
         return
@@ -503,6 +591,7 @@ def run_ours(args):
 
     ssim_line = None if args.skip_ssim else ssim_workload(args, dev, stream)
     loss_line = None if args.skip_loss else loss_workload(args, dev)
+    stream_line = None if args.skip_stream else stream_workload(args, dev)
 
     if rank == 0:
         line = {
@@ -532,6 +621,8 @@ def run_ours(args):
             line["ivssim"] = ssim_line
         if loss_line:
             line["loss"] = loss_line
+        if stream_line:
+            line["stream"] = stream_line
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_sample()
         print(json.dumps(line))
@@ -546,10 +637,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="multiview", choices=["multiview", "small", "ssim", "loss"],
+    ap.add_argument("--workload", default="multiview", choices=["multiview", "small", "ssim", "loss", "stream"],
                     help="small: the 24-pair 1080p case used for ncu captures")
     ap.add_argument("--skip-ssim", action="store_true", help="skip the IV-SSIM / SSIM / MS-SSIM workload")
     ap.add_argument("--skip-loss", action="store_true", help="skip the differentiable-loss forward/backward workload")
+    ap.add_argument("--skip-stream", action="store_true", help="skip the streamed 8K ERP sequence workload")
     ap.add_argument("--kernels-only", action="store_true",
                     help="time only the batched launches (for profiler captures)")
     args = ap.parse_args()

@@ -199,3 +199,22 @@ def test_batch_mixed_sizes(gpu_lib, oq):
             for i, (ora, ws) in enumerate(oras):
                 r = _abi.FrameResult.from_buffer_copy(host[i * ctypes.sizeof(_abi.FrameResult):(i + 1) * ctypes.sizeof(_abi.FrameResult)])
                 _cmp(r.to_dict(), ora)
+
+
+def test_8k_erp_sr4_matches_oracle(gpu_lib, oq):
+    """The streamed-sequence picture size: 7680x3840 ERP 10-bit, search range 4, device input."""
+    import torch
+    w, h, bd = 7680, 3840, 10
+    ref, tst = synth.pair420(w, h, bd, seed=synth.seed_for(4, 0, 0), holes=True)
+    d0 = [torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in synth.split420(ref, w, h)]
+    d1 = [torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in synth.split420(tst, w, h)]
+    with gpu_lib.Processor(w, h, search_range=4, use_ws=True, scratch_metrics=gpu_lib.M_PSNR | gpu_lib.M_WSPSNR | gpu_lib.M_IVPSNR) as P:
+        g = P.calc_frame(gpu_lib.make_pic(d0, bd), gpu_lib.make_pic(d1, bd), gpu_lib.M_PSNR | gpu_lib.M_WSPSNR | gpu_lib.M_IVPSNR)
+    from oracle.oracle import upsample420
+    o = oq.frame(upsample420(synth.split420(ref, w, h), w, h), upsample420(synth.split420(tst, w, h), w, h), bd, False,
+                 use_ws=True, search_range=4, nthreads=16)
+    assert g["gcd_r2t"][:3] == o["gcd"]
+    assert g["sse_r2t"][:3] == o["sse_r2t"] and g["sse_t2r"][:3] == o["sse_t2r"]
+    for k in ("ivpsnr", "ivpsnr_r2t", "ivpsnr_t2r"):
+        assert abs(g[k] - o[k]) <= 1e-10
+    assert max(abs(a - b) for a, b in zip(g["wspsnr"][:3], o["wspsnr"])) <= 1e-10
