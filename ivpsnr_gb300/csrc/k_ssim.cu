@@ -239,6 +239,184 @@ __global__ void __launch_bounds__(kThreads, 3) k_ssim(const SsimJob* __restrict_
   }
 }
 
+// ---- the full-resolution family of a component in one pass -----------------------------------
+// Picture 0, picture 1 and the two shift-compensated pictures share their window sums: ten
+// moment streams (S1 of the four planes; S(a^2+b^2) and S(ab) of the three pairs (P0,P1),
+// (P0,SCP1), (P1,SCP0)) give SSIM, CS, IV-SSIM T2R and R2T, against sixteen for four separate
+// pair evaluations. Tiles are 16 rows high (the ten streams' vertical sums fill shared memory
+// faster); the staging is (P0, P1, SCP1, SCP0) float4 per sample, centred by the tile-centre
+// sample of P1.
+constexpr int kQTY = 16, kQPairs = 5;
+template <int WIN> struct QGeo {
+  static constexpr int TX = kIW - WIN + 1;
+  static constexpr int IH = kQTY + WIN - 1;
+  static constexpr int RPW = (IH + 7) / 8;
+  // staged [IH][64] float4; vertical sums [5][16][kRP] float2; row sums [4][7][16] float
+  static constexpr int SMEM = IH * kIW * 16 + kQPairs * kQTY * kRP * 8 + 4 * 7 * kQTY * 4;
+  static_assert(4 * 14 >= TX && 4 * 13 + 3 + WIN - 1 < kRP, "tile columns");
+};
+
+__device__ __forceinline__ float ssim_index(float S1a, float S1b, float Sq, float Sx, float om2c, float omc,
+                                            float k_cc, float cw0, float C1, float C2, bool calc_l)
+{
+  const float sab = S1a + S1b;
+  const float den_cs = fmaf(-S1b, S1b, fmaf(-S1a, S1a, Sq)) + fmaf(om2c, sab, fmaf(2.0f, k_cc, C2));
+  const float cov = fmaf(-S1a, S1b, Sx) + fmaf(omc, sab, k_cc);
+  float num = fmaf(2.0f, cov, C2), den = den_cs;
+  if(calc_l)
+  { // L * CS = (nL nCS) / (dL dCS): one division (xStructSim.cpp:50-51)
+    const float mua = S1a + cw0, mub = S1b + cw0;
+    num *= fmaf(2.0f * mua, mub, C1);
+    den *= fmaf(mua, mua, fmaf(mub, mub, C1));
+  }
+  return __fdividef(num, den);
+}
+
+template <int WIN>
+__global__ void __launch_bounds__(kThreads, 3) k_ssim_quad(const SsimQuadJob* __restrict__ jobs, int njobs, int ntiles)
+{
+  using G = QGeo<WIN>;
+  extern __shared__ __align__(16) float smem[];
+  float4* s_in = reinterpret_cast<float4*>(smem);                                  // [IH][64]
+  float2* s_v = reinterpret_cast<float2*>(smem + 4 * G::IH * kIW);                // [5][16][kRP]
+  float* s_red = smem + 4 * G::IH * kIW + 2 * kQPairs * kQTY * kRP;               // [4][7][16]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  float2 gk[WIN];
+  #pragma unroll
+  for(int k = 0; k < WIN; k++)
+  {
+    gk[k] = c_g2[k];
+    asm volatile("" : "+f"(gk[k].x), "+f"(gk[k].y));
+  }
+  const int wi = WIN == 11 ? 1 : 0;
+  int jb = 0;
+  for(int tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+  {
+    while(jb + 1 < njobs && jobs[jb + 1].tile_base <= tile) jb++;
+    const SsimQuadJob& J = jobs[jb];
+    const int local = tile - J.tile_base;
+    const int ty = local / J.tiles_x, tx = local - ty * J.tiles_x;
+    const int x0 = 5 + tx * G::TX, y0 = 5 + ty * kQTY;
+    const int x1 = min(x0 + G::TX, J.W - 5), y1 = min(y0 + kQTY, J.H - 5);
+    // staging: all loads first, centring offset = the tile-centre sample of picture 1
+    float v0[G::RPW][2], v1[G::RPW][2], v2[G::RPW][2], v3[G::RPW][2];
+    const float tc = ld_plane(J.p1, min((x0 + x1) >> 1, J.W - 1), min((y0 + y1) >> 1, J.H - 1));
+    load_plane<G::IH>(J.p0, v0, x0 - 5, y0 - 5, J.W, J.H);
+    load_plane<G::IH>(J.p1, v1, x0 - 5, y0 - 5, J.W, J.H);
+    load_plane<G::IH>(J.scp1, v2, x0 - 5, y0 - 5, J.W, J.H);
+    load_plane<G::IH>(J.scp0, v3, x0 - 5, y0 - 5, J.W, J.H);
+    #pragma unroll
+    for(int k = 0; k < G::RPW; k++)
+    {
+      const int i = warp + 8 * k;
+      if(i < G::IH)
+      {
+        s_in[i * kIW + lane] = make_float4(v0[k][0] - tc, v1[k][0] - tc, v2[k][0] - tc, v3[k][0] - tc);
+        s_in[i * kIW + lane + 32] = make_float4(v0[k][1] - tc, v1[k][1] - tc, v2[k][1] - tc, v3[k][1] - tc);
+      }
+    }
+    __syncthreads();
+
+    // vertical pass: column q, output rows 4rg .. 4rg+3; five float2 stream pairs
+    {
+      const int q = tid & (kIW - 1), rg = tid >> 6;
+      const float4* src = s_in + 4 * rg * kIW + q;
+      float2 acc[4][kQPairs];
+      #pragma unroll
+      for(int o = 0; o < 4; o++)
+        #pragma unroll
+        for(int m = 0; m < kQPairs; m++) acc[o][m] = make_float2(0.f, 0.f);
+      #pragma unroll
+      for(int i = 0; i < 3 + WIN; i++)
+      {
+        const float4 v = src[i * kIW];          // P0, P1, SCP1, SCP0
+        const float2 sq01 = __fmul2_rn(make_float2(v.x, v.y), make_float2(v.x, v.y));
+        const float2 sq23 = __fmul2_rn(make_float2(v.z, v.w), make_float2(v.z, v.w));
+        float2 st[kQPairs];
+        st[0] = make_float2(v.x, v.y);
+        st[1] = make_float2(v.z, v.w);
+        st[2] = make_float2(sq01.x + sq01.y, v.x * v.y);   // (P0, P1)
+        st[3] = make_float2(sq01.x + sq23.x, v.x * v.z);   // (P0, SCP1)
+        st[4] = make_float2(sq01.y + sq23.y, v.y * v.w);   // (P1, SCP0)
+        #pragma unroll
+        for(int o = 0; o < 4; o++)
+        {
+          const int k = i - o;
+          if(k < 0 || k >= WIN) continue;
+          #pragma unroll
+          for(int m = 0; m < kQPairs; m++) acc[o][m] = __ffma2_rn(gk[k], st[m], acc[o][m]);
+        }
+      }
+      #pragma unroll
+      for(int o = 0; o < 4; o++)
+        #pragma unroll
+        for(int m = 0; m < kQPairs; m++) s_v[(m * kQTY + 4 * rg + o) * kRP + q] = acc[o][m];
+    }
+    __syncthreads();
+
+    // horizontal pass and the indices: row o (lanes 0-15 / 16-31), output columns 4gi .. 4gi+3
+    if(warp < 7)
+    {
+      const int o = lane & 15, gi = 2 * warp + (lane >> 4), j0 = 4 * gi;
+      float2 m[4][kQPairs];
+      #pragma unroll
+      for(int jj = 0; jj < 4; jj++)
+        #pragma unroll
+        for(int s2 = 0; s2 < kQPairs; s2++) m[jj][s2] = make_float2(0.f, 0.f);
+      #pragma unroll
+      for(int t = 0; t < 3 + WIN; t++)
+      {
+        float2 val[kQPairs];
+        #pragma unroll
+        for(int s2 = 0; s2 < kQPairs; s2++) val[s2] = s_v[(s2 * kQTY + o) * kRP + j0 + t];
+        #pragma unroll
+        for(int jj = 0; jj < 4; jj++)
+        {
+          const int k = t - jj;
+          if(k < 0 || k >= WIN) continue;
+          #pragma unroll
+          for(int s2 = 0; s2 < kQPairs; s2++) m[jj][s2] = __ffma2_rn(gk[k], val[s2], m[jj][s2]);
+        }
+      }
+      const float cf = tc;
+      const float k_cc = (float)(c_omd[wi] * (double)tc * (double)tc * c_w0d[wi]);
+      const float cw0 = cf * c_w0[wi], om2c = c_om[wi] * 2.0f * cf, omc = c_om[wi] * cf;
+      const float C1 = J.c1, C2 = J.c2;
+      const bool row_ok = y0 + o < y1;
+      float rs[4] = { 0.f, 0.f, 0.f, 0.f };
+      #pragma unroll
+      for(int jj = 0; jj < 4; jj++)
+      {
+        if(!(row_ok && x0 + j0 + jj < x1)) continue;
+        const float S0 = m[jj][0].x, S1 = m[jj][0].y, Ss1 = m[jj][1].x, Ss0 = m[jj][1].y;
+        if(J.outs & 1u) rs[0] += ssim_index(S0, S1, m[jj][2].x, m[jj][2].y, om2c, omc, k_cc, cw0, C1, C2, true);
+        if(J.outs & 2u) rs[1] += ssim_index(S0, S1, m[jj][2].x, m[jj][2].y, om2c, omc, k_cc, cw0, C1, C2, false);
+        if(J.outs & 4u) rs[2] += ssim_index(S0, Ss1, m[jj][3].x, m[jj][3].y, om2c, omc, k_cc, cw0, C1, C2, true);
+        if(J.outs & 8u) rs[3] += ssim_index(S1, Ss0, m[jj][4].x, m[jj][4].y, om2c, omc, k_cc, cw0, C1, C2, true);
+      }
+      #pragma unroll
+      for(int k = 0; k < 4; k++)
+      {
+        const float v = rs[k] + __shfl_xor_sync(0xffffffffu, rs[k], 16);
+        if(lane < 16) s_red[(k * 7 + warp) * kQTY + o] = v;
+      }
+    }
+    __syncthreads();
+    if(tid < 4 * kQTY)
+    { // output k, row r of the tile: fixed-order sum over the 7 column warps
+      const int k = tid >> 4, r = tid & 15;
+      if(J.outs & (1u << k))
+      {
+        float s = 0.0f;
+        #pragma unroll
+        for(int w = 0; w < 7; w++) s += s_red[(k * 7 + w) * kQTY + r];
+        const int y = y0 + r;
+        if(y < y1) J.partial[k][(int64_t)(y - 5) * J.tiles_x + tx] = s;
+      }
+    }
+  }
+}
+
 // Picture sum of one SSIM job: rows summed over their tiles in FP64 (fixed order), rows combined
 // with a compensated sum, divided by W*H (xSSIM.cpp:106-111).
 __global__ void __launch_bounds__(256) k_ssim_finalize(const SsimJob* __restrict__ jobs, int njobs)
@@ -592,6 +770,35 @@ cudaError_t launch_ssim_bwd(const SsimBwdJob* d_jobs, const SsimBwdJob* h_jobs, 
   }
   if(window == QMIV_SSIM_GAUSS11) k_ssim_bwd<11><<<blocks, 256, BGeo<11>::SMEM, st>>>(d_jobs, n);
   else                            k_ssim_bwd<10><<<blocks, 256, BGeo<10>::SMEM, st>>>(d_jobs, n);
+  return cudaGetLastError();
+}
+
+int ssim_quad_tiles_y(int H) { return H > 10 ? (H - 10 + kQTY - 1) / kQTY : 0; }
+
+cudaError_t launch_ssim_quad(const SsimQuadJob* d_jobs, const SsimQuadJob* h_jobs, int n, int window, cudaStream_t st)
+{
+  int tiles = 0;
+  for(int i = 0; i < n; i++) tiles = h_jobs[i].tile_base + h_jobs[i].tiles_x * h_jobs[i].tiles_y;
+  if(tiles == 0) return cudaSuccess;
+  static int resident[2] = { 0, 0 };
+  static int sms = 0;
+  const int wi = window == QMIV_SSIM_GAUSS11 ? 1 : 0;
+  if(!resident[wi])
+  {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if(e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_quad<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, QGeo<10>::SMEM);
+    if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_quad<11>, cudaFuncAttributeMaxDynamicSharedMemorySize, QGeo<11>::SMEM);
+    if(e == cudaSuccess)
+      e = wi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[1], k_ssim_quad<11>, kThreads, QGeo<11>::SMEM)
+             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[0], k_ssim_quad<10>, kThreads, QGeo<10>::SMEM);
+    if(e != cudaSuccess) return e;
+    if(resident[wi] < 1) resident[wi] = 1;
+  }
+  const int grid = std::min(tiles, sms * resident[wi]);
+  if(wi) k_ssim_quad<11><<<grid, kThreads, QGeo<11>::SMEM, st>>>(d_jobs, n, tiles);
+  else   k_ssim_quad<10><<<grid, kThreads, QGeo<10>::SMEM, st>>>(d_jobs, n, tiles);
   return cudaGetLastError();
 }
 

@@ -125,6 +125,7 @@ struct qmiv_handle {
   // host-side working copies of the tables
   std::vector<DevJob> jobs;
   std::vector<SsimJob> sjobs;
+  std::vector<SsimQuadJob> qjobs;         // fused full-resolution SSIM family (IV-SSIM frames)
   std::vector<PyrStep> steps[4];
   std::vector<SsimFrame> frames;
   // staging for host pictures (2 pictures, planar, up to uint16 4:4:4)
@@ -485,19 +486,41 @@ qmiv_status plan_ssim(qmiv_handle* h, const DevJob& j)
   float* part = S.partial;
   const SsimPlane P0[3] = { plane_of(j.p0[0], j.stride0[0], sb, 0), plane_of(j.p0[1], j.stride0[1], sb, cs), plane_of(j.p0[2], j.stride0[2], sb, cs) };
   const SsimPlane P1[3] = { plane_of(j.p1[0], j.stride1[0], sb, 0), plane_of(j.p1[1], j.stride1[1], sb, cs), plane_of(j.p1[2], j.stride1[2], sb, cs) };
-  if(j.metrics & QMIV_M_SSIM)   // xAppQMIV.cpp:907: calcPicSSIM(P0, P1)
-    for(int c = 0; c < 3; c++) add_ssim_job(h, P0[c], P1[c], W, H, bd, 1, part, S.vals + c);
-  if(j.metrics & QMIV_M_IVSSIM) // xSSIM.cpp:197-198: T2R = SSIM(P0, SCP1), R2T = SSIM(P1, SCP0)
-  {
+  if(j.metrics & QMIV_M_IVSSIM)
+  { // one fused pass per component: SSIM(P0,P1), CS(P0,P1) (MS-SSIM scale 0), and the IV-SSIM
+    // directions T2R = SSIM(P0, SCP1), R2T = SSIM(P1, SCP0) (xSSIM.cpp:197-198); each output is
+    // finalised by an SsimJob entry without tiles of its own
+    const double mx = (double)((1 << bd) - 1);
     for(int c = 0; c < 3; c++)
     {
-      add_ssim_job(h, P0[c], plane_of(j.scp1[c], j.scp_stride, 2, 0), W, H, bd, 1, part, S.vals + 18 + c);
-      add_ssim_job(h, P1[c], plane_of(j.scp0[c], j.scp_stride, 2, 0), W, H, bd, 1, part, S.vals + 21 + c);
+      SsimQuadJob q;
+      std::memset(&q, 0, sizeof(q));
+      q.p0 = P0[c]; q.p1 = P1[c];
+      q.scp1 = plane_of(j.scp1[c], j.scp_stride, 2, 0);
+      q.scp0 = plane_of(j.scp0[c], j.scp_stride, 2, 0);
+      q.W = W; q.H = H;
+      q.c1 = (float)((0.01 * mx) * (0.01 * mx)); // xSSIM.cpp:21-23
+      q.c2 = (float)((0.03 * mx) * (0.03 * mx));
+      q.tiles_x = ssim_tiles_x(W, h->opt.ssim_window);
+      q.tiles_y = ssim_quad_tiles_y(H);
+      q.outs = ((j.metrics & QMIV_M_SSIM) ? 1u : 0u) | ((j.metrics & QMIV_M_MSSSIM) ? 2u : 0u) | 12u;
+      double* outs[4] = { S.vals + c, S.vals + 3 + c, S.vals + 18 + c, S.vals + 21 + c };
+      for(int k = 0; k < 4; k++)
+      {
+        if(!(q.outs & (1u << k))) continue;
+        q.partial[k] = part;
+        add_ssim_job(h, P0[c], P1[c], W, H, bd, 1, part, outs[k]);
+        h->sjobs.back().tiles_y = 0;  // finalisation only
+      }
+      h->qjobs.push_back(q);
     }
   }
+  else if(j.metrics & QMIV_M_SSIM)   // xAppQMIV.cpp:907: calcPicSSIM(P0, P1)
+    for(int c = 0; c < 3; c++) add_ssim_job(h, P0[c], P1[c], W, H, bd, 1, part, S.vals + c);
   if(j.metrics & QMIV_M_MSSSIM) // xSSIM.cpp:67-87
   {
-    for(int c = 0; c < 3; c++) add_ssim_job(h, P0[c], P1[c], W, H, bd, 0, part, S.vals + 3 + c);
+    if(!(j.metrics & QMIV_M_IVSSIM))
+      for(int c = 0; c < 3; c++) add_ssim_job(h, P0[c], P1[c], W, H, bd, 0, part, S.vals + 3 + c);
     // pyramid: level s of picture p, component c lives at pyr + off(s) + (p*3+c)*cap(s)
     size_t off = 0;
     SsimPlane prev[2][3];
@@ -551,6 +574,7 @@ size_t pack_tables(const qmiv_handle* h, uint8_t* dst, size_t cap)
   put(h->sjobs.data(), sizeof(SsimJob) * h->sjobs.size());
   for(int s = 0; s < 4; s++) put(h->steps[s].data(), sizeof(PyrStep) * h->steps[s].size());
   put(h->frames.data(), sizeof(SsimFrame) * h->frames.size());
+  put(h->qjobs.data(), sizeof(SsimQuadJob) * h->qjobs.size());
   return ok ? pos : 0;
 }
 
@@ -612,12 +636,14 @@ qmiv_status plan_jobs(qmiv_handle* h, LaunchPlan& P, cudaStream_t st)
     }
   }
   h->jobs = sorted;
-  h->sjobs.clear(); h->frames.clear();
+  h->sjobs.clear(); h->frames.clear(); h->qjobs.clear();
   for(int s = 0; s < 4; s++) h->steps[s].clear();
   for(int i = 0; i < n; i++)
     if(h->jobs[i].metrics & kSsimMetrics) { qmiv_status ps = plan_ssim(h, h->jobs[i]); if(ps != QMIV_OK) return ps; }
   int tb = 0;
   for(auto& s : h->sjobs) { s.tile_base = tb; tb += s.tiles_x * s.tiles_y; }
+  tb = 0;
+  for(auto& q : h->qjobs) { q.tile_base = tb; tb += q.tiles_x * q.tiles_y; }
   return QMIV_OK;
 }
 
@@ -667,6 +693,15 @@ qmiv_status launch_jobs(qmiv_handle* h, const LaunchPlan& P, const uint8_t* d_ta
       pos += align256(sizeof(PyrStep) * h->steps[s].size());
     }
     const SsimFrame* d_frames = reinterpret_cast<const SsimFrame*>(d_tab + pos);
+    pos += align256(sizeof(SsimFrame) * h->frames.size());
+    if(!h->qjobs.empty())
+    {
+      const SsimQuadJob* d_q = reinterpret_cast<const SsimQuadJob*>(d_tab + pos);
+      CUDA_TRY(prof_mark(h, h->opt.ssim_window == QMIV_SSIM_GAUSS11 ? "k_ssim_quad<11>" : "k_ssim_quad<10>", st, true));
+      CUDA_TRY(launch_ssim_quad(d_q, h->qjobs.data(), (int)h->qjobs.size(), h->opt.ssim_window, st));
+      CUDA_TRY(prof_mark(h, nullptr, st, false));
+      h->launches++;
+    }
     const SsimJob* d_sjobs = reinterpret_cast<const SsimJob*>(d_tab + align256(sizeof(DevJob) * n));
     CUDA_TRY(prof_mark(h, h->opt.ssim_window == QMIV_SSIM_GAUSS11 ? "k_ssim<11>" : "k_ssim<10>", st, true));
     CUDA_TRY(launch_ssim(d_sjobs, h->sjobs.data(), (int)h->sjobs.size(), h->opt.ssim_window, st));
@@ -842,7 +877,8 @@ qmiv_status qmiv_create(qmiv_handle** out, const qmiv_options* opt, int32_t max_
   CallTables& t = h->tab;
   t.jobs_off = 0;
   t.bytes = align256(sizeof(DevJob) * max_jobs) + align256(sizeof(SsimJob) * kSsimJobsPerFrame * max_jobs) +
-            4 * align256(sizeof(PyrStep) * kPyrStepsPerFrame * max_jobs) + align256(sizeof(SsimFrame) * max_jobs);
+            4 * align256(sizeof(PyrStep) * kPyrStepsPerFrame * max_jobs) + align256(sizeof(SsimFrame) * max_jobs) +
+            align256(sizeof(SsimQuadJob) * 3 * max_jobs);
   if(cudaMalloc(&h->d_tab, t.bytes) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "call tables"));
   for(int k = 0; k < qmiv_handle::kRing; k++)
   {

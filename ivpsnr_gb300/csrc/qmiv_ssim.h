@@ -28,6 +28,22 @@ struct SsimJob {
   double* out;           // picture mean
 };
 
+// The full-resolution SSIM family of one component of one frame in a single pass over its
+// four planes: picture 0, picture 1 and the two shift-compensated pictures. Outputs (bits of
+// `outs`): 0 SSIM(P0, P1) (L*CS), 1 CS(P0, P1) (MS-SSIM scale 0), 2 SSIM(P0, SCP1) (IV-SSIM T2R),
+// 3 SSIM(P1, SCP0) (IV-SSIM R2T). Each output's per-tile row sums go to partial[k] in the
+// layout of an SsimJob with the same picture size.
+struct SsimQuadJob {
+  SsimPlane p0, p1, scp1, scp0;
+  int32_t W, H;
+  float c1, c2;
+  int32_t tiles_x, tiles_y, tile_base;
+  uint32_t outs;
+  float* partial[4];
+};
+int ssim_quad_tiles_y(int H);
+cudaError_t launch_ssim_quad(const SsimQuadJob* d_jobs, const SsimQuadJob* h_jobs, int n, int window, cudaStream_t st);
+
 // One DownsampleHV step of the MS-SSIM pyramid.
 struct PyrStep {
   SsimPlane src;

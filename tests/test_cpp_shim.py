@@ -46,6 +46,8 @@ def test_cpp_processors_match_the_c_abi(gpu_lib, tmp_path, w, h, erp):
     assert got["gcd"] == want["gcd_r2t"][:3]
     assert got["psnr"] == want["psnr"][:3] and got["wspsnr"] == want["wspsnr"][:3]
     assert got["ivpsnr"] == want["ivpsnr"]
-    np.testing.assert_allclose(got["ssim"], want["ssim"][:3], rtol=0, atol=1e-12)
-    np.testing.assert_allclose(got["msssim"], want["msssim"][:3], rtol=0, atol=1e-12)
-    assert abs(got["ivssim"] - want["ivssim"]) <= 1e-12
+    # calc_frame evaluates the IV-SSIM frame family in one fused pass, the shim in separate calls:
+    # both FP32 forms are within 1e-6 of the FP64 oracle, and within 1e-7 of each other
+    np.testing.assert_allclose(got["ssim"], want["ssim"][:3], rtol=0, atol=1e-7)
+    np.testing.assert_allclose(got["msssim"], want["msssim"][:3], rtol=0, atol=1e-7)
+    assert abs(got["ivssim"] - want["ivssim"]) <= 1e-7
