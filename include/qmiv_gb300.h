@@ -255,6 +255,32 @@ qmiv_status qmiv_loss_backward(const float* tst, const float* ref, int32_t n, in
                                const qmiv_options* opt, void* workspace, size_t workspace_bytes,
                                const double* g_sse, const double* g_ssim, float* g_tst, qmiv_stream stream);
 
+/* --- input side ------------------------------------------------------------------------
+ * Range check and concealment (xPixelOps::CheckIfInRange / ClipToRange, libs/pmbb-core/src/
+ * xPixelOpsSTD.cpp:163-209, as xAppQMIV::validateFrames applies them, apps/QMIV/src/
+ * xAppQMIV.cpp:753-770): counts the samples of each component above 2^bitdepth - 1 in a device
+ * picture; with conceal != 0 clips them in place (the planes must be writable). Synchronous. */
+qmiv_status qmiv_check_range(const qmiv_pic* pic, int32_t conceal, int64_t out_of_range[3], qmiv_stream stream);
+/* Fixed-point colour conversion of a device 4:4:4 picture (xColorSpace::ConvertRGB2YCbCr /
+ * ConvertYCbCr2RGB, xColorSpaceSTD.cpp:195-272, as xAppQMIV::preprocessFrames uses it,
+ * xAppQMIV.cpp:778-814): to_ycbcr 1 reads R, G, B planes and writes Y, Cb, Cr; 0 the reverse.
+ * color_space: 0 BT.601, 1 BT.709, 2 SMPTE 240M, 3 BT.2020. dst: three device uint16 planes
+ * with row pitch dst_stride (samples); they may be src's own planes (in place, as the application
+ * converts) when src has 16-bit samples and dst_stride is its stride. Asynchronous on stream. */
+qmiv_status qmiv_color_convert(const qmiv_pic* src, uint16_t* dst[3], int32_t dst_stride, int32_t to_ycbcr,
+                               int32_t color_space, qmiv_stream stream);
+/* Raw planar YUV files (xSeqBase, libs/pmbb-core/src/xSeq.cpp:179-250): 8-bit samples as bytes,
+ * deeper ones as 16-bit little endian, chroma 420, 422 or 444. qmiv_yuv_read seeks frame,
+ * reads it into pinned memory and uploads it on stream into one of two device buffers (frame
+ * parity), returning a device qmiv_pic valid until the read of frame + 2; 4:2:2 chroma is
+ * doubled horizontally on the device into 4:4:4 planes (UpsampleH), 4:2:0 stays native. */
+typedef struct qmiv_yuv_reader qmiv_yuv_reader;
+qmiv_status qmiv_yuv_open(qmiv_yuv_reader** out, const char* path, int32_t width, int32_t height, int32_t bitdepth,
+                          int32_t chroma_format);
+int64_t     qmiv_yuv_frames(const qmiv_yuv_reader* r);
+qmiv_status qmiv_yuv_read(qmiv_yuv_reader* r, int64_t frame, qmiv_pic* out, qmiv_stream stream);
+qmiv_status qmiv_yuv_close(qmiv_yuv_reader* r);
+
 /* --- per sequence ----------------------------------------------------------------------
  * xMetricStat::calcAvgMetric (xAppQMIV.h:256-260): compensated mean over the frames passed
  * to qmiv_calc_frame since create or the last reset. */

@@ -91,6 +91,12 @@ SIGNATURES = [
     ("qmiv_loss_forward", c_i32, [_vp, _vp, c_i32, c_i32, c_i32, _P(Options), _vp, ctypes.c_size_t, _vp, _vp, _vp]),
     ("qmiv_loss_backward", c_i32, [_vp, _vp, c_i32, c_i32, c_i32, _P(Options), _vp, ctypes.c_size_t, _vp, _vp, _vp,
                                    _vp]),
+    ("qmiv_check_range", c_i32, [_P(Pic), c_i32, _P(ctypes.c_int64), _vp]),
+    ("qmiv_color_convert", c_i32, [_P(Pic), _P(_vp), c_i32, c_i32, c_i32, _vp]),
+    ("qmiv_yuv_open", c_i32, [_P(_vp), ctypes.c_char_p, c_i32, c_i32, c_i32, c_i32]),
+    ("qmiv_yuv_frames", ctypes.c_int64, [_vp]),
+    ("qmiv_yuv_read", c_i32, [_vp, ctypes.c_int64, _P(Pic), _vp]),
+    ("qmiv_yuv_close", c_i32, [_vp]),
     ("qmiv_finish_sequence", c_i32, [_vp, _P(SeqResult)]),
     ("qmiv_reset_sequence", c_i32, [_vp]),
     ("qmiv_kernel_launches", ctypes.c_int64, [_vp]),

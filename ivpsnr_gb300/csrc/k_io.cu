@@ -1,0 +1,151 @@
+// Input-side kernels around the metric path (all HBM bound, one thread per sample or pixel):
+//   * 4:2:2 to 4:4:4 horizontal nearest-neighbour upsampling of raw frames
+//     (xSeqBase::xUnpackFrame, libs/pmbb-core/src/xSeq.cpp:179-250, UpsampleH semantics);
+//   * range check and concealment of out-of-range samples (xPixelOpsSTD::CheckIfInRange /
+//     ClipToRange, libs/pmbb-core/src/xPixelOpsSTD.cpp:163-209, as xAppQMIV::validateFrames uses
+//     them, apps/QMIV/src/xAppQMIV.cpp:753-770);
+//   * fixed-point RGB <-> YCbCr conversion (xColorSpaceSTD::ConvertRGB2YCbCr_I32 /
+//     ConvertYCbCr2RGB_I32, libs/pmbb-core/src/xColorSpaceSTD.cpp:195-272), 16-bit fraction.
+#include "qmiv_io.h"
+
+namespace qmiv {
+
+namespace {
+
+__device__ __forceinline__ int ld(const void* p, int sb, int64_t o)
+{
+  return sb == 1 ? (int)__ldg((const uint8_t*)p + o) : (int)__ldg((const uint16_t*)p + o);
+}
+
+// plain (coherent) load, for planes the same kernel writes (in-place clipping and conversion)
+__device__ __forceinline__ int ld_rw(const void* p, int sb, int64_t o)
+{
+  return sb == 1 ? (int)((const uint8_t*)p)[o] : (int)((const uint16_t*)p)[o];
+}
+
+// dst (W x H, pitch W) from a chroma plane of W/2 x H: dst(x, y) = src(x >> 1, y)
+__global__ void k_upsample_h(const void* __restrict__ src, int sbytes, int sstride, void* __restrict__ dst, int W, int H)
+{
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  if(x >= W || y >= H) return;
+  const int v = ld(src, sbytes, (int64_t)y * sstride + (x >> 1));
+  if(sbytes == 1) ((uint8_t*)dst)[(int64_t)y * W + x] = (uint8_t)v;
+  else            ((uint16_t*)dst)[(int64_t)y * W + x] = (uint16_t)v;
+}
+
+// count samples above Max in one plane; optionally clip them in place
+__global__ void __launch_bounds__(256) k_range(void* plane, int sbytes, int stride, int w, int h, int maxv, int conceal,
+                                               unsigned long long* count)
+{
+  __shared__ unsigned int s_n[8];
+  unsigned int n = 0;
+  const int64_t total = (int64_t)w * h;
+  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x)
+  {
+    const int y = (int)(i / w), x = (int)(i - (int64_t)y * w);
+    const int64_t o = (int64_t)y * stride + x;
+    const int v = ld_rw(plane, sbytes, o);
+    if(v > maxv)
+    {
+      n++;
+      if(conceal)
+      {
+        if(sbytes == 1) ((uint8_t*)plane)[o] = (uint8_t)maxv;
+        else            ((uint16_t*)plane)[o] = (uint16_t)maxv;
+      }
+    }
+  }
+  for(int d = 16; d > 0; d >>= 1) n += __shfl_xor_sync(0xffffffffu, n, d);
+  if((threadIdx.x & 31) == 0) s_n[threadIdx.x >> 5] = n;
+  __syncthreads();
+  if(threadIdx.x == 0)
+  {
+    unsigned int t = 0;
+    for(int k = 0; k < 8; k++) t += s_n[k];
+    if(t) atomicAdd(count, (unsigned long long)t);
+  }
+}
+
+__device__ __forceinline__ int clipu(int v, int mx) { return v < 0 ? 0 : (v > mx ? mx : v); }
+
+__global__ void k_color(ColorJob J)
+{
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  if(x >= J.W || y >= J.H) return;
+  const int64_t so = (int64_t)y * J.sstride + x, dof = (int64_t)y * J.dstride + x;
+  const int a = ld_rw(J.src[0], J.sbytes, so), b = ld_rw(J.src[1], J.sbytes, so), c = ld_rw(J.src[2], J.sbytes, so);
+  const int mid = 1 << (J.bd - 1), mx = (1 << J.bd) - 1;
+  int o0, o1, o2;
+  if(J.to_ycbcr)
+  { // a, b, c = R, G, B (xColorSpaceSTD.cpp:195-232)
+    const int ty = (J.m[0][0] * a + J.m[0][1] * b + J.m[0][2] * c + kColorAdd) >> kColorPrec;
+    const int tu = (J.m[1][0] * a + J.m[1][1] * b + (c << (kColorPrec - 1)) + kColorAdd) >> kColorPrec;
+    const int tv = ((a << (kColorPrec - 1)) + J.m[2][1] * b + J.m[2][2] * c + kColorAdd) >> kColorPrec;
+    o0 = clipu(ty, mx); o1 = clipu(tu + mid, mx); o2 = clipu(tv + mid, mx);
+  }
+  else
+  { // a, b, c = Y, Cb, Cr (xColorSpaceSTD.cpp:234-272)
+    const int iu = b - mid, iv = c - mid;
+    const int sy = (a << kColorPrec) + kColorAdd;
+    o0 = clipu((sy + J.m[0][2] * iv) >> kColorPrec, mx);
+    o1 = clipu((sy + J.m[1][1] * iu + J.m[1][2] * iv) >> kColorPrec, mx);
+    o2 = clipu((sy + J.m[2][1] * iu) >> kColorPrec, mx);
+  }
+  J.dst[0][dof] = (uint16_t)o0;
+  J.dst[1][dof] = (uint16_t)o1;
+  J.dst[2][dof] = (uint16_t)o2;
+}
+
+}  // namespace
+
+void color_matrix(int space, bool to_ycbcr, int32_t m[3][3])
+{ // base coefficients (Kr, Kg, Kb) of BT.601, BT.709, SMPTE 240M, BT.2020 (xColorSpaceCoeff.h:36-42)
+  static const double base[4][3] = { { 0.299, 0.587, 0.114 }, { 0.2126, 0.7152, 0.0722 },
+                                     { 0.2120, 0.7010, 0.0870 }, { 0.2627, 0.6780, 0.0593 } };
+  const double kr = base[space][0], kg = base[space][1], kb = base[space][2];
+  double d[3][3];
+  if(to_ycbcr)
+  {
+    const double sb = 0.5 / (kb - 1.0), sr = 0.5 / (kr - 1.0);
+    const double t[3][3] = { { kr, kg, kb }, { sb * kr, sb * kg, 0.5 }, { 0.5, sr * kg, sr * kb } };
+    for(int i = 0; i < 3; i++) for(int j = 0; j < 3; j++) d[i][j] = t[i][j];
+  }
+  else
+  {
+    const double t[3][3] = { { 1.0, 0.0, 2 - 2 * kr },
+                             { 1.0, 2.0 * (kb * kb - kb) / kg, 2.0 * (kr * kr - kr) / kg },
+                             { 1.0, 2 - 2 * kb, 0.0 } };
+    for(int i = 0; i < 3; i++) for(int j = 0; j < 3; j++) d[i][j] = t[i][j];
+  }
+  // 2^16 fraction bits, rounded half away from zero
+  for(int i = 0; i < 3; i++)
+    for(int j = 0; j < 3; j++)
+    {
+      const double v = 65536.0 * d[i][j];
+      m[i][j] = v >= 0.0 ? (int32_t)(v + 0.5) : -(int32_t)(-v + 0.5);
+    }
+}
+
+cudaError_t launch_upsample_h(const void* src, int sbytes, int sstride, void* dst, int W, int H, cudaStream_t st)
+{
+  k_upsample_h<<<dim3((W + 255) / 256, H), 256, 0, st>>>(src, sbytes, sstride, dst, W, H);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_range(void* plane, int sbytes, int stride, int w, int h, int maxv, int conceal, unsigned long long* count,
+                         int sms, cudaStream_t st)
+{
+  const int64_t total = (int64_t)w * h;
+  int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)sms * 8);
+  if(blocks < 1) blocks = 1;
+  k_range<<<blocks, 256, 0, st>>>(plane, sbytes, stride, w, h, maxv, conceal, count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_color(const ColorJob& j, cudaStream_t st)
+{
+  k_color<<<dim3((j.W + 255) / 256, j.H), 256, 0, st>>>(j);
+  return cudaGetLastError();
+}
+
+}  // namespace qmiv

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include "qmiv_internal.h"
+#include "qmiv_io.h"
 #include "qmiv_loss.h"
 #include "qmiv_masked.h"
 #include "qmiv_ssim.h"
@@ -1548,5 +1549,176 @@ qmiv_status qmiv_loss_backward(const float* tst, const float* ref, int32_t n, in
   if(s != QMIV_OK) return s;
   if(!g_sse || !g_ssim || !g_tst) return fail(QMIV_BAD_ARG, "loss: null gradients");
   CUDA_TRY(loss_backward(a, g_sse, g_ssim, g_tst, (cudaStream_t)stream));
+  return QMIV_OK;
+}
+
+// ------------------------------------------------------------------------------------
+// Input side: range check / concealment, colour conversion, raw YUV reader
+// ------------------------------------------------------------------------------------
+static int device_sms()
+{
+  int dev = 0, sms = 0;
+  if(cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  return sms;
+}
+
+static qmiv_status check_device_pic(const qmiv_pic* p, const char* name)
+{
+  if(!p) return fail(QMIV_BAD_ARG, "%s is null", name);
+  if(!p->is_device) return fail(QMIV_BAD_ARG, "%s must be in device memory", name);
+  if(p->width < 1 || p->height < 1) return fail(QMIV_BAD_ARG, "%s: size %dx%d", name, p->width, p->height);
+  if(p->bitdepth < 1 || p->bitdepth > 16) return fail(QMIV_BAD_ARG, "%s: bit depth %d", name, p->bitdepth);
+  if(p->sample_bytes != 1 && p->sample_bytes != 2) return fail(QMIV_BAD_ARG, "%s: sample_bytes %d", name, p->sample_bytes);
+  if(p->chroma_format != QMIV_CF420 && p->chroma_format != QMIV_CF444) return fail(QMIV_UNSUPPORTED, "%s: chroma format %d", name, p->chroma_format);
+  for(int c = 0; c < 3; c++)
+  {
+    const int w = (c && p->chroma_format == QMIV_CF420) ? p->width / 2 : p->width;
+    if(!p->plane[c] || p->stride[c] < w) return fail(QMIV_BAD_ARG, "%s: plane %d null or stride < width", name, c);
+  }
+  return QMIV_OK;
+}
+
+qmiv_status qmiv_check_range(const qmiv_pic* pic, int32_t conceal, int64_t out_of_range[3], qmiv_stream stream)
+{
+  qmiv_status s = check_device_pic(pic, "pic");
+  if(s != QMIV_OK) return s;
+  if(!out_of_range) return fail(QMIV_BAD_ARG, "out_of_range is null");
+  const cudaStream_t st = (cudaStream_t)stream;
+  unsigned long long* d_cnt = nullptr;
+  CUDA_TRY(cudaMallocAsync((void**)&d_cnt, 3 * sizeof(unsigned long long), st));
+  CUDA_TRY(cudaMemsetAsync(d_cnt, 0, 3 * sizeof(unsigned long long), st));
+  const int maxv = pic->bitdepth >= 16 ? 65535 : (1 << pic->bitdepth) - 1;
+  const int sms = device_sms();
+  for(int c = 0; c < 3; c++)
+  {
+    const bool sub = c && pic->chroma_format == QMIV_CF420;
+    CUDA_TRY(launch_range(const_cast<void*>(pic->plane[c]), pic->sample_bytes, pic->stride[c], sub ? pic->width / 2 : pic->width,
+                          sub ? pic->height / 2 : pic->height, maxv, conceal ? 1 : 0, d_cnt + c, sms, st));
+  }
+  unsigned long long h[3];
+  CUDA_TRY(cudaMemcpyAsync(h, d_cnt, sizeof(h), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaFreeAsync(d_cnt, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  for(int c = 0; c < 3; c++) out_of_range[c] = (int64_t)h[c];
+  return QMIV_OK;
+}
+
+qmiv_status qmiv_color_convert(const qmiv_pic* src, uint16_t* dst[3], int32_t dst_stride, int32_t to_ycbcr,
+                               int32_t color_space, qmiv_stream stream)
+{
+  qmiv_status s = check_device_pic(src, "src");
+  if(s != QMIV_OK) return s;
+  if(src->chroma_format != QMIV_CF444) return fail(QMIV_UNSUPPORTED, "colour conversion works on 4:4:4 pictures");
+  if(src->bitdepth > 14) return fail(QMIV_UNSUPPORTED, "colour conversion: bit depth %d (at most 14)", src->bitdepth);
+  if(color_space < 0 || color_space > 3) return fail(QMIV_BAD_ARG, "colour space %d (0 BT.601, 1 BT.709, 2 SMPTE 240M, 3 BT.2020)", color_space);
+  if(!dst || !dst[0] || !dst[1] || !dst[2] || dst_stride < src->width) return fail(QMIV_BAD_ARG, "dst planes or stride");
+  if(src->stride[0] != src->stride[1] || src->stride[0] != src->stride[2]) return fail(QMIV_UNSUPPORTED, "src planes must share one stride");
+  ColorJob j;
+  std::memset(&j, 0, sizeof(j));
+  for(int c = 0; c < 3; c++) { j.src[c] = src->plane[c]; j.dst[c] = dst[c]; }
+  j.sbytes = src->sample_bytes; j.sstride = src->stride[0]; j.dstride = dst_stride;
+  j.W = src->width; j.H = src->height; j.bd = src->bitdepth; j.to_ycbcr = to_ycbcr ? 1 : 0;
+  color_matrix(color_space, to_ycbcr != 0, j.m);
+  CUDA_TRY(launch_color(j, (cudaStream_t)stream));
+  return QMIV_OK;
+}
+
+struct qmiv_yuv_reader {
+  FILE* f = nullptr;
+  int32_t w = 0, h = 0, bd = 8, cf = 420, bps = 1;
+  int64_t frame_bytes = 0, frames = 0;
+  uint8_t* h_buf[2] = { nullptr, nullptr };   // pinned, one per device slot
+  uint8_t* d_raw[2] = { nullptr, nullptr };   // the raw frame as read
+  uint8_t* d_444[2] = { nullptr, nullptr };   // 4:2:2 chroma upsampled to 4:4:4
+  cudaEvent_t ev[2] = { nullptr, nullptr };
+  bool used[2] = { false, false };
+};
+
+qmiv_status qmiv_yuv_close(qmiv_yuv_reader* r)
+{
+  if(!r) return QMIV_OK;
+  if(r->f) std::fclose(r->f);
+  for(int i = 0; i < 2; i++)
+  {
+    if(r->ev[i]) { cudaEventSynchronize(r->ev[i]); cudaEventDestroy(r->ev[i]); }
+    cudaFreeHost(r->h_buf[i]); cudaFree(r->d_raw[i]); cudaFree(r->d_444[i]);
+  }
+  delete r;
+  return QMIV_OK;
+}
+
+qmiv_status qmiv_yuv_open(qmiv_yuv_reader** out, const char* path, int32_t width, int32_t height, int32_t bitdepth,
+                          int32_t chroma_format)
+{
+  if(!out || !path) return fail(QMIV_BAD_ARG, "out or path is null");
+  *out = nullptr;
+  if(width < 1 || height < 1 || bitdepth < 1 || bitdepth > 16) return fail(QMIV_BAD_ARG, "size %dx%d, bit depth %d", width, height, bitdepth);
+  if(chroma_format != 420 && chroma_format != 422 && chroma_format != 444) return fail(QMIV_UNSUPPORTED, "chroma format %d (420, 422, 444)", chroma_format);
+  if((chroma_format != 444 && (width & 1)) || (chroma_format == 420 && (height & 1))) return fail(QMIV_UNSUPPORTED, "odd size for %d", chroma_format);
+  qmiv_yuv_reader* r = new qmiv_yuv_reader;
+  auto bail = [&](qmiv_status e) { qmiv_yuv_close(r); return e; };
+  r->w = width; r->h = height; r->bd = bitdepth; r->cf = chroma_format; r->bps = bitdepth > 8 ? 2 : 1;
+  const int64_t area = (int64_t)width * height;
+  const int64_t csz = chroma_format == 420 ? area / 4 : (chroma_format == 422 ? area / 2 : area);
+  r->frame_bytes = (area + 2 * csz) * r->bps;
+  r->f = std::fopen(path, "rb");
+  if(!r->f) return bail(fail(QMIV_BAD_ARG, "cannot open %s", path));
+  std::fseek(r->f, 0, SEEK_END);
+  const long long bytes = std::ftell(r->f);
+  r->frames = bytes / r->frame_bytes;  // xSeqBase counts whole frames
+  for(int i = 0; i < 2; i++)
+  {
+    if(cudaMallocHost((void**)&r->h_buf[i], r->frame_bytes) != cudaSuccess ||
+       cudaMalloc((void**)&r->d_raw[i], r->frame_bytes) != cudaSuccess ||
+       cudaEventCreateWithFlags(&r->ev[i], cudaEventDisableTiming) != cudaSuccess)
+      return bail(fail(QMIV_OUT_OF_MEMORY, "YUV reader buffers"));
+    if(chroma_format == 422 && cudaMalloc((void**)&r->d_444[i], 2 * area * r->bps) != cudaSuccess)
+      return bail(fail(QMIV_OUT_OF_MEMORY, "YUV reader 4:4:4 chroma"));
+  }
+  *out = r;
+  return QMIV_OK;
+}
+
+int64_t qmiv_yuv_frames(const qmiv_yuv_reader* r) { return r ? r->frames : 0; }
+
+qmiv_status qmiv_yuv_read(qmiv_yuv_reader* r, int64_t frame, qmiv_pic* out, qmiv_stream stream)
+{
+  if(!r || !out) return fail(QMIV_BAD_ARG, "reader or out is null");
+  if(frame < 0 || frame >= r->frames) return fail(QMIV_BAD_ARG, "frame %lld of %lld", (long long)frame, (long long)r->frames);
+  const cudaStream_t st = (cudaStream_t)stream;
+  const int k = (int)(frame & 1);
+  if(r->used[k]) CUDA_TRY(cudaEventSynchronize(r->ev[k]));  // the slot's previous upload has finished
+  if(std::fseek(r->f, (long)(frame * r->frame_bytes), SEEK_SET) != 0 ||
+     std::fread(r->h_buf[k], 1, (size_t)r->frame_bytes, r->f) != (size_t)r->frame_bytes)
+    return fail(QMIV_BAD_ARG, "short read of frame %lld", (long long)frame);
+  CUDA_TRY(cudaMemcpyAsync(r->d_raw[k], r->h_buf[k], (size_t)r->frame_bytes, cudaMemcpyHostToDevice, st));
+  const int64_t area = (int64_t)r->w * r->h;
+  const int bps = r->bps;
+  std::memset(out, 0, sizeof(*out));
+  out->width = r->w; out->height = r->h; out->bitdepth = r->bd; out->sample_bytes = bps; out->is_device = 1;
+  out->plane[0] = r->d_raw[k]; out->stride[0] = r->w;
+  if(r->cf == 420)
+  {
+    out->chroma_format = QMIV_CF420;
+    out->plane[1] = r->d_raw[k] + area * bps; out->plane[2] = r->d_raw[k] + (area + area / 4) * bps;
+    out->stride[1] = out->stride[2] = r->w / 2;
+  }
+  else if(r->cf == 444)
+  {
+    out->chroma_format = QMIV_CF444;
+    out->plane[1] = r->d_raw[k] + area * bps; out->plane[2] = r->d_raw[k] + 2 * area * bps;
+    out->stride[1] = out->stride[2] = r->w;
+  }
+  else
+  { // 4:2:2: chroma doubled horizontally into 4:4:4 planes (xSeq.cpp:219-233)
+    for(int c = 0; c < 2; c++)
+      CUDA_TRY(launch_upsample_h(r->d_raw[k] + (area + c * area / 2) * bps, bps, r->w / 2, r->d_444[k] + c * area * bps,
+                                 r->w, r->h, st));
+    out->chroma_format = QMIV_CF444;
+    out->plane[1] = r->d_444[k]; out->plane[2] = r->d_444[k] + area * bps;
+    out->stride[1] = out->stride[2] = r->w;
+  }
+  CUDA_TRY(cudaEventRecord(r->ev[k], st));
+  r->used[k] = true;
   return QMIV_OK;
 }

@@ -67,6 +67,9 @@ for p in "${pids[@]}"; do wait "$p"; done
 # the checker harness (this repository's code, linked against the reference objects)
 g++ "${CXXFLAGS[@]}" "$HERE/ref_harness.cpp" "${objs[@]}" -lpthread -o "$OUT/qmiv_ref_harness"
 
+# the checker of the input-side operations (colour conversion, range check / clipping)
+g++ "${CXXFLAGS[@]}" "$HERE/ref_io.cpp" "${objs[@]}" -lpthread -o "$OUT/qmiv_ref_io"
+
 # the reference's own command-line tool, to reproduce its published example values
 APP_OBJS=()
 for f in "$SRC/apps/QMIV/src/main_QMIV.cpp" "$SRC/apps/QMIV/src/xAppQMIV.cpp" "$SRC"/libs/pmbb-spng/src/*.cpp; do

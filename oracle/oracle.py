@@ -73,6 +73,11 @@ def lib():
                                        P(ctypes.c_int32), P(OqOpts), ctypes.c_void_p,
                                        P(ctypes.c_double), P(ctypes.c_double)]
         L.oq_ivpsnr_masked.restype = ctypes.c_double
+        L.oq_color_matrix.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p]
+        L.oq_color_convert.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                       ctypes.c_int32, ctypes.c_int32]
+        L.oq_range_clip.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32]
+        L.oq_range_clip.restype = ctypes.c_int64
         _LIB = L
     return _LIB
 
@@ -227,3 +232,35 @@ def masked(p0, p1, mask, bd, mask_bd=8, use_ws=False, lat_range_deg=180, **kw):
     wsp = [fake if exact[c] else wsp[c] for c in range(3)]
     return {"nnm": nnm, "gcd": list(g), "psnr": psnr, "wspsnr": wsp, "ivpsnr": iv,
             "ivpsnr_r2t": r2t.value, "ivpsnr_t2r": t2r.value, "exact": exact}
+
+
+def color_convert(planes, bd, space, to_ycbcr):
+    """xColorSpaceSTD::ConvertRGB2YCbCr_I32 / ConvertYCbCr2RGB_I32 of three uint16 planes."""
+    src = np.ascontiguousarray(np.stack(planes), np.uint16)
+    _, h, w = src.shape
+    out = np.zeros_like(src)
+    lib().oq_color_convert(src.ctypes.data, out.ctypes.data, w, h, bd, space, int(to_ycbcr))
+    return out
+
+
+def color_matrix(space, to_ycbcr):
+    m = (ctypes.c_int32 * 9)()
+    lib().oq_color_matrix(space, int(to_ycbcr), m)
+    return [list(m[0:3]), list(m[3:6]), list(m[6:9])]
+
+
+def range_clip(plane, bd):
+    """(number of samples above 2^bd - 1, the clipped plane)."""
+    p = np.ascontiguousarray(plane, np.uint16).copy()
+    h, w = p.shape
+    n = lib().oq_range_clip(p.ctypes.data, w, h, bd)
+    return int(n), p
+
+
+def unpack_frame(raw, w, h, bps, cf):
+    """xSeqBase::xUnpackFrame of one raw planar frame (bytes): (3, H, W) uint16, 4:4:4."""
+    buf = np.frombuffer(raw, np.uint8)
+    out = np.zeros((3, h, w), np.uint16)
+    if lib().oq_unpack_frame(buf.ctypes.data, w, h, bps, cf, out.ctypes.data) != 0:
+        raise ValueError("unsupported frame layout")
+    return out

@@ -84,6 +84,20 @@ int oq_unpack_frame(const uint8_t* packed, int32_t w, int32_t h, int32_t bps, in
     }
     return 0;
   }
+  if(cf == 422)
+  { /* UpsampleH (xSeq.cpp:219-233): chroma planes (w/2) x h, doubled horizontally */
+    if(w & 1) return -1;
+    const int32_t cw = w >> 1;
+    const size_t carea = area >> 1;
+    for(int c = 0; c < 2; c++)
+    {
+      const uint8_t* src = chroma + c * carea * bps;
+      uint16_t* dst = out + (c + 1) * area;
+      for(int32_t y = 0; y < h; y++)
+        for(int32_t x = 0; x < w; x++) dst[(size_t)y * w + x] = SAMPLE(src, (size_t)y * cw + (x >> 1));
+    }
+    return 0;
+  }
   #undef SAMPLE
   return -1;
 }
@@ -565,4 +579,72 @@ double oq_ivpsnr_masked(const oq_pic* p0, const oq_pic* p1, const uint16_t* mask
   if(r2t_out) *r2t_out = r2t;
   if(t2r_out) *t2r_out = t2r;
   return t2r < r2t ? t2r : r2t;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* input-side operations                                                                 */
+/* ------------------------------------------------------------------------------------ */
+/* xColorSpaceCoeff::xRnd (xColorSpaceCoeff.h:172-176): round half away from zero */
+static int32_t color_rnd(double v) { return v >= 0.0 ? (int32_t)(v + 0.5) : -(int32_t)(-v + 0.5); }
+
+/* fixed-point matrices (xColorSpaceCoeff.h:36-100,178-203), 16 fraction bits */
+void oq_color_matrix(int32_t space, int32_t to_ycbcr, int32_t m[3][3])
+{
+  static const double base[4][3] = { { 0.299, 0.587, 0.114 }, { 0.2126, 0.7152, 0.0722 },
+                                     { 0.2120, 0.7010, 0.0870 }, { 0.2627, 0.6780, 0.0593 } };
+  const double kr = base[space][0], kg = base[space][1], kb = base[space][2];
+  double d[3][3];
+  if(to_ycbcr)
+  {
+    const double sb = 0.5 / (kb - 1.0), sr = 0.5 / (kr - 1.0);
+    const double t[3][3] = { { kr, kg, kb }, { sb * kr, sb * kg, 0.5 }, { 0.5, sr * kg, sr * kb } };
+    memcpy(d, t, sizeof(d));
+  }
+  else
+  {
+    const double t[3][3] = { { 1.0, 0.0, 2 - 2 * kr },
+                             { 1.0, 2.0 * (kb * kb - kb) / kg, 2.0 * (kr * kr - kr) / kg },
+                             { 1.0, 2 - 2 * kb, 0.0 } };
+    memcpy(d, t, sizeof(d));
+  }
+  for(int i = 0; i < 3; i++)
+    for(int j = 0; j < 3; j++) m[i][j] = color_rnd(65536.0 * d[i][j]);
+}
+
+/* xColorSpaceSTD::ConvertRGB2YCbCr_I32 / ConvertYCbCr2RGB_I32 (xColorSpaceSTD.cpp:195-272) */
+void oq_color_convert(const uint16_t* in, uint16_t* out, int32_t w, int32_t h, int32_t bd, int32_t space, int32_t to_ycbcr)
+{
+  int32_t m[3][3];
+  oq_color_matrix(space, to_ycbcr, m);
+  const size_t a = (size_t)w * h;
+  const int32_t mid = 1 << (bd - 1), mx = maxval(bd), add = 1 << 15;
+  for(size_t i = 0; i < a; i++)
+  {
+    const int32_t p = in[i], q = in[a + i], r = in[2 * a + i];
+    int32_t o0, o1, o2;
+    if(to_ycbcr)
+    {
+      o0 = clampi((m[0][0] * p + m[0][1] * q + m[0][2] * r + add) >> 16, 0, mx);
+      o1 = clampi(((m[1][0] * p + m[1][1] * q + (r << 15) + add) >> 16) + mid, 0, mx);
+      o2 = clampi((((p << 15) + m[2][1] * q + m[2][2] * r + add) >> 16) + mid, 0, mx);
+    }
+    else
+    {
+      const int32_t iu = q - mid, iv = r - mid, sy = (p << 16) + add;
+      o0 = clampi((sy + m[0][2] * iv) >> 16, 0, mx);
+      o1 = clampi((sy + m[1][1] * iu + m[1][2] * iv) >> 16, 0, mx);
+      o2 = clampi((sy + m[2][1] * iu) >> 16, 0, mx);
+    }
+    out[i] = (uint16_t)o0; out[a + i] = (uint16_t)o1; out[2 * a + i] = (uint16_t)o2;
+  }
+}
+
+/* xPixelOpsSTD::CheckIfInRange + ClipToRange (xPixelOpsSTD.cpp:163-209): returns the number of
+   samples above 2^bd - 1 and clips them in place */
+int64_t oq_range_clip(uint16_t* p, int32_t w, int32_t h, int32_t bd)
+{
+  const int32_t mx = maxval(bd);
+  int64_t n = 0;
+  for(size_t i = 0; i < (size_t)w * h; i++) if(p[i] > mx) { n++; p[i] = (uint16_t)mx; }
+  return n;
 }

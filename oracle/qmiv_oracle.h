@@ -107,6 +107,11 @@ double oq_ivpsnr_masked(const oq_pic* p0, const oq_pic* p1, const uint16_t* mask
                         const int32_t gcd_r2t[3], const oq_opts* o, const double* ws_weights,
                         double* r2t, double* t2r);
 
+/* input-side operations: colour conversion (xColorSpaceSTD.cpp:195-272), range clip (xPixelOpsSTD.cpp:163-209) */
+void    oq_color_matrix(int32_t space, int32_t to_ycbcr, int32_t m[3][3]);
+void    oq_color_convert(const uint16_t* in, uint16_t* out, int32_t w, int32_t h, int32_t bd, int32_t space, int32_t to_ycbcr);
+int64_t oq_range_clip(uint16_t* p, int32_t w, int32_t h, int32_t bd);
+
 #ifdef __cplusplus
 }
 #endif

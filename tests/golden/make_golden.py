@@ -21,6 +21,7 @@ sys.path.insert(0, ROOT)
 from ivpsnr_gb300 import synth  # noqa: E402
 
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "qmiv_ref_harness")
+IO_CHECKER = os.path.join(ROOT, "oracle", "_ref", "qmiv_ref_io")
 
 # name, w, h, bd, seed, generator kwargs, harness options
 CASES = [
@@ -97,6 +98,41 @@ def run_masked_case(name, w, h, bd, seed, gkw, hopt, kind, tmp):
     }
 
 
+def io_inputs(kind, w, h, bd, seed):
+    """Deterministic inputs of the input-side cases: three uint16 planes (colour) or one plane
+    with some samples above the bit depth's peak (range)."""
+    rng = np.random.default_rng(seed)
+    if kind == "color":
+        return rng.integers(0, 1 << bd, (3, h, w)).astype(np.uint16)
+    return rng.integers(0, (1 << bd) + (1 << bd) // 8, (h, w)).astype(np.uint16)
+
+
+def run_io_cases(tmp):
+    cases = []
+    w, h = 64, 32
+    for space in range(4):
+        for to in (1, 0):
+            for bd in (8, 10):
+                seed = 1000 + space * 10 + to * 2 + bd
+                x = io_inputs("color", w, h, bd, seed)
+                a, b = os.path.join(tmp, "c_in.raw"), os.path.join(tmp, "c_out.raw")
+                x.tofile(a)
+                subprocess.check_call([IO_CHECKER, "color", str(space), str(to), str(bd), str(w), str(h), a, b])
+                y = np.fromfile(b, np.uint16).reshape(3, h, w)
+                cases.append({"kind": "color", "space": space, "to_ycbcr": to, "bd": bd, "w": w, "h": h, "seed": seed,
+                              "input_md5": md5(x), "output_md5": md5(y), "output_head": y[:, 0, :8].tolist()})
+    for bd in (8, 10, 12):
+        seed = 2000 + bd
+        x = io_inputs("range", w, h, bd, seed)
+        a, b = os.path.join(tmp, "r_in.raw"), os.path.join(tmp, "r_out.raw")
+        x.tofile(a)
+        out = json.loads(subprocess.check_output([IO_CHECKER, "range", str(bd), str(w), str(h), a, b]).decode())
+        y = np.fromfile(b, np.uint16).reshape(h, w)
+        cases.append({"kind": "range", "bd": bd, "w": w, "h": h, "seed": seed, "input_md5": md5(x), "in_range": out["in_range"],
+                      "output_md5": md5(y)})
+    return cases
+
+
 def md5(*arrays):
     h = hashlib.md5()
     for a in arrays:
@@ -147,6 +183,12 @@ def main():
         json.dump({"generator": "ivpsnr_gb300.synth.pair420 + make_golden.make_mask",
                    "reference": "pmbb-ivqm via oracle/ref_harness.cpp -im", "cases": masked}, f, indent=1)
     print("wrote", path, len(masked), "masked cases")
+    io = run_io_cases(tmp)
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "io.json")
+    with open(path, "w") as f:
+        json.dump({"generator": "make_golden.io_inputs", "reference": "xColorSpace / xPixelOps via oracle/ref_io.cpp",
+                   "cases": io}, f, indent=1)
+    print("wrote", path, len(io), "input-side cases")
 
 
 if __name__ == "__main__":
