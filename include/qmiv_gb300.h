@@ -108,7 +108,8 @@ typedef struct qmiv_seq_result {
 
 /* One job of a batch: a picture pair plus the metrics to compute on it. Pictures of a
  * batch may differ in size, bit depth and chroma format; use_ws selects ERP weighting
- * per job (lat_deg from the options). Device pointers only. */
+ * per job (lat_deg from the options). Device pictures for qmiv_calc_batch, host pictures for
+ * qmiv_calc_batch_host. */
 typedef struct qmiv_job {
   qmiv_pic pic0, pic1;
   uint32_t metrics;
@@ -170,6 +171,18 @@ qmiv_status qmiv_calc_frame_masked(qmiv_handle* h, const qmiv_pic* pic0, const q
  * to the sequence statistics. */
 qmiv_status qmiv_calc_batch(qmiv_handle* h, const qmiv_job* jobs, int32_t n, qmiv_frame_result* results,
                             qmiv_stream stream);
+
+/* Batched form for host pictures (the pictures of every job in host memory, page-locked for the
+ * copies to overlap): the handle uploads the jobs in consecutive groups of at most group_bytes
+ * of packed planes (0: a sixteenth of the batch, and a quarter of that for the last eighth of the
+ * batch, whose measurement no upload hides; never less than the largest job) into two device
+ * buffers it owns, on an upload stream of its own, and measures each group on `stream` as
+ * qmiv_calc_batch does while the next group uploads. Asynchronous: returns once everything is
+ * enqueued; the host pictures must stay unchanged until `stream` synchronises, after which the
+ * results (device memory, n entries) are valid. Groups hold at most max_jobs jobs. No reference
+ * counterpart: it replaces the application's read-then-measure loop over many pictures. */
+qmiv_status qmiv_calc_batch_host(qmiv_handle* h, const qmiv_job* jobs, int32_t n, qmiv_frame_result* results,
+                                 size_t group_bytes, qmiv_stream stream);
 
 /* A batch captured once as a CUDA graph and replayed: for a fixed set of device pictures whose
  * contents change between replays (video frames decoded into the same buffers). No

@@ -152,6 +152,13 @@ class Processor:
         arr = (_abi.Job * len(jobs))(*jobs)
         _abi.check(self.lib.qmiv_calc_batch(self.h, arr, len(jobs), results_ptr, stream), "qmiv_calc_batch")
 
+    def calc_batch_host(self, jobs, results_ptr, group_bytes=0, stream=0):
+        """qmiv_calc_batch_host: jobs with host (pinned) pictures, uploaded in groups overlapped with
+        the measurement; results_ptr is device memory; asynchronous on stream."""
+        arr = (_abi.Job * len(jobs))(*jobs)
+        _abi.check(self.lib.qmiv_calc_batch_host(self.h, arr, len(jobs), results_ptr, group_bytes, stream),
+                   "qmiv_calc_batch_host")
+
     def capture_batch(self, jobs, results_ptr, stream):
         """qmiv_batch_graph_create: the batch recorded once as a CUDA graph; returns a BatchGraph."""
         arr = (_abi.Job * len(jobs))(*jobs)

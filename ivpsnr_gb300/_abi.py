@@ -76,6 +76,7 @@ SIGNATURES = [
     ("qmiv_calc_frame", c_i32, [_vp, _P(Pic), _P(Pic), c_u32, _P(FrameResult), _vp]),
     ("qmiv_calc_frame_masked", c_i32, [_vp, _P(Pic), _P(Pic), _P(Mask), c_u32, _P(FrameResult), _vp]),
     ("qmiv_calc_batch", c_i32, [_vp, _P(Job), c_i32, _vp, _vp]),
+    ("qmiv_calc_batch_host", c_i32, [_vp, _P(Job), c_i32, _vp, ctypes.c_size_t, _vp]),
     ("qmiv_batch_graph_create", c_i32, [_vp, _P(Job), c_i32, _vp, _vp, _P(_vp)]),
     ("qmiv_batch_graph_launch", c_i32, [_vp, _vp]),
     ("qmiv_batch_graph_destroy", c_i32, [_vp]),

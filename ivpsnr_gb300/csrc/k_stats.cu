@@ -10,6 +10,7 @@
 // 4:2:0). For 4:2:0 the chroma sums of the 4:4:4 picture the reference works on are exact
 // multiples of the native chroma sums (each chroma sample is replicated 2x2,
 // xPixelOpsSTD.cpp:30-49), so the upsampled planes are never formed.
+#include <cstddef>
 #include <mutex>
 
 #include "qmiv_device.cuh"
@@ -227,6 +228,42 @@ __global__ void __launch_bounds__(kStatsThreads) k_stats(const DevJob* __restric
     __threadfence();
     finalize_stats(J, p, scratch);
   }
+}
+
+// Every job's result entry cleared and stamped with its metric set before the metric kernels
+// write their fields, so that the fields of metrics not requested read as zero.
+__global__ void __launch_bounds__(256) k_init_results(const DevJob* __restrict__ jobs, int n)
+{
+  constexpr int kWords = (int)(sizeof(qmiv_frame_result) / 4);
+  for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n * kWords; i += gridDim.x * blockDim.x)
+  {
+    const int j = i / kWords, w = i - j * kWords;
+    reinterpret_cast<uint32_t*>(jobs[j].result)[w] = w == 0 ? jobs[j].metrics : 0u;
+  }
+}
+
+// A call's tables copied from page-locked host memory by the SMs, not the copy engine: a copy
+// engine runs its copies in order, so a small table copy would otherwise wait behind large
+// picture uploads queued earlier on another stream.
+__global__ void __launch_bounds__(256) k_copy_table(const uint4* __restrict__ src, uint4* __restrict__ dst, int n16)
+{
+  for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += gridDim.x * blockDim.x) dst[i] = src[i];
+}
+
+cudaError_t launch_copy_table(const void* src, void* dst, size_t bytes, cudaStream_t st)
+{
+  const int n16 = (int)(bytes / 16);
+  if(n16 == 0) return cudaSuccess;
+  k_copy_table<<<std::min(152, (n16 + 255) / 256), 256, 0, st>>>(static_cast<const uint4*>(src), static_cast<uint4*>(dst), n16);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_init_results(const DevJob* d_jobs, int n, cudaStream_t st)
+{
+  static_assert(sizeof(qmiv_frame_result) % 4 == 0 && offsetof(qmiv_frame_result, metrics) == 0, "result layout");
+  const int words = n * (int)(sizeof(qmiv_frame_result) / 4);
+  k_init_results<<<std::min(64, (words + 255) / 256), 256, 0, st>>>(d_jobs, n);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_stats(const DevJob* d_jobs, const DevJob* h_jobs, int n, const Params& p, cudaStream_t st)

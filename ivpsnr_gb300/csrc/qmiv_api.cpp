@@ -84,9 +84,13 @@ struct Slot {
   int64_t* stat_rows = nullptr;           // [max_h][6]
   unsigned long long* cps_rows = nullptr; // [2][max_h][3]
   JobScalars* sc = nullptr;
-  void* d_tmaps = nullptr;                // 6 x 128 B
-  uint64_t tmap_key[16] = { 0 };
-  bool tmap_valid = false;
+  // encoded tensor-map sets of the last kTmapSets picture layouts this slot ran (6 x 128 B each,
+  // device), so that a batch repeated over alternating buffers finds its maps without a copy
+  static constexpr int kTmapSets = 16;
+  uint8_t* d_tmaps = nullptr;
+  uint64_t tmap_key[kTmapSets][16] = { { 0 } };
+  uint64_t tmap_stamp[kTmapSets] = { 0 };
+  bool tmap_valid[kTmapSets] = { false };
   uint16_t* scp = nullptr;                // 2 pictures x 3 planes x max_w*max_h (IV-SSIM)
   uint16_t* pyr = nullptr;                // MS-SSIM levels 1..4, 2 pictures x 3 components
   float* partial = nullptr;               // SSIM per-tile row sums of all the frame's SSIM jobs
@@ -119,7 +123,8 @@ struct qmiv_handle {
   CallTables tab;
   uint8_t* d_tab = nullptr;
   static constexpr int kRing = 4;
-  uint8_t* h_tab[kRing] = { nullptr };
+  uint8_t* h_tab[kRing] = { nullptr };      // page-locked, mapped
+  uint8_t* h_tab_dev[kRing] = { nullptr };  // their device addresses
   cudaEvent_t tab_ev[kRing] = { nullptr };
   bool tab_used[kRing] = { false };
   int tab_next = 0;
@@ -131,6 +136,19 @@ struct qmiv_handle {
   std::vector<SsimFrame> frames;
   // staging for host pictures (2 pictures, planar, up to uint16 4:4:4)
   uint16_t* d_stage[2] = { nullptr, nullptr };
+  // qmiv_calc_batch_host: its upload stream, two device group buffers and their events
+  cudaStream_t up_stream = nullptr;
+  uint8_t* d_up[2] = { nullptr, nullptr };
+  size_t up_cap = 0;
+  cudaEvent_t up_done[2] = { nullptr, nullptr }, up_free[2] = { nullptr, nullptr };
+  bool up_recorded[2] = { false, false };
+  // pinned staging ring of encoded tensor maps (6 per entry), so that re-encoding a job's maps
+  // never waits for the stream: an entry is rewritten only after its copy has run
+  uint8_t* h_tmaps = nullptr;
+  std::vector<cudaEvent_t> tmap_ev;
+  std::vector<char> tmap_used;
+  int tmap_next = 0;
+  uint64_t tmap_clock = 0;                // LRU stamps of the slots' tensor-map sets
   // masked frames: per-row sums, counters / count / GCD, host-mask staging
   int64_t* mask_rows = nullptr;
   uint8_t* mask_small = nullptr;
@@ -369,27 +387,72 @@ void plan_grid(qmiv_handle* h, DevJob* jobs, int n, const std::vector<int>& vari
   }
 }
 
-qmiv_status upload_pic(qmiv_handle* h, const qmiv_pic* src, int idx, qmiv_pic* dst, cudaStream_t st)
-{ // host picture -> packed device staging (same sample size, planes back to back, 16-byte rows aligned)
-  *dst = *src;
-  if(src->is_device) return QMIV_OK;
-  const int sb = src->sample_bytes;
-  uint8_t* base = reinterpret_cast<uint8_t*>(h->d_stage[idx]);
+// Device bytes of a host picture packed as stage_pic lays it out.
+size_t stage_bytes(const qmiv_pic* p)
+{
   size_t off = 0;
+  const int sb = p->sample_bytes;
+  for(int c = 0; c < 3; c++)
+  {
+    const int w = (c && p->chroma_format == QMIV_CF420) ? p->width / 2 : p->width;
+    const int hh = (c && p->chroma_format == QMIV_CF420) ? p->height / 2 : p->height;
+    off = (off + 255) & ~(size_t)255;
+    off += (size_t)(((w * sb + 15) & ~15)) * hh;
+  }
+  return (off + 255) & ~(size_t)255;
+}
+
+// Host picture -> packed device copy at base (same sample size, planes back to back and
+// 256-byte aligned, rows padded to 16-byte multiples so that the TMA kernels can take them).
+// A plane whose rows are contiguous on both sides goes as one linear copy, and planes stored
+// back to back on both sides (a picture held as one Y-Cb-Cr buffer) as one copy: the copy
+// engine pays a fixed cost per copy and moves short pitched rows well below its linear rate.
+// The merged range is exactly the planes' bytes; if the runtime refuses it (the planes are
+// separate page-locked allocations that happen to touch), the planes go one by one.
+qmiv_status stage_pic(const qmiv_pic* src, uint8_t* base, qmiv_pic* dst, cudaStream_t st)
+{
+  *dst = *src;
+  const int sb = src->sample_bytes;
+  size_t off = 0;
+  struct Run { const uint8_t* s; uint8_t* d; size_t bytes; };
+  Run runs[3];
+  int nr = 0;
   for(int c = 0; c < 3; c++)
   {
     const int w = (c && src->chroma_format == QMIV_CF420) ? src->width / 2 : src->width;
     const int hh = (c && src->chroma_format == QMIV_CF420) ? src->height / 2 : src->height;
-    const int pitch = ((w * sb + 15) & ~15) / sb;  // rows of 16-byte multiples: TMA-eligible
-    off = (off + 15) & ~(size_t)15;
-    CUDA_TRY(cudaMemcpy2DAsync(base + off, (size_t)pitch * sb, src->plane[c], (size_t)src->stride[c] * sb,
-                               (size_t)w * sb, hh, cudaMemcpyHostToDevice, st));
+    const int pitch = ((w * sb + 15) & ~15) / sb;
+    off = (off + 255) & ~(size_t)255;
+    const uint8_t* sp = static_cast<const uint8_t*>(src->plane[c]);
+    if(src->stride[c] == w && pitch == w)
+      runs[nr++] = { sp, base + off, (size_t)w * hh * sb };
+    else
+      CUDA_TRY(cudaMemcpy2DAsync(base + off, (size_t)pitch * sb, sp, (size_t)src->stride[c] * sb,
+                                 (size_t)w * sb, hh, cudaMemcpyHostToDevice, st));
     dst->plane[c] = base + off;
     dst->stride[c] = pitch;
     off += (size_t)pitch * hh * sb;
   }
+  int k = 0;
+  while(k < nr)
+  {
+    int e = k;
+    size_t bytes = runs[k].bytes;
+    while(e + 1 < nr && runs[e + 1].s == runs[k].s + bytes && runs[e + 1].d == runs[k].d + bytes) bytes += runs[++e].bytes;
+    if(e > k && cudaMemcpyAsync(runs[k].d, runs[k].s, bytes, cudaMemcpyHostToDevice, st) == cudaSuccess) { k = e + 1; continue; }
+    if(e > k) (void)cudaGetLastError();  // refused merge: clear it and copy plane by plane
+    for(int i = k; i <= e; i++) CUDA_TRY(cudaMemcpyAsync(runs[i].d, runs[i].s, runs[i].bytes, cudaMemcpyHostToDevice, st));
+    k = e + 1;
+  }
   dst->is_device = 1;
   return QMIV_OK;
+}
+
+qmiv_status upload_pic(qmiv_handle* h, const qmiv_pic* src, int idx, qmiv_pic* dst, cudaStream_t st)
+{
+  *dst = *src;
+  if(src->is_device) return QMIV_OK;
+  return stage_pic(src, reinterpret_cast<uint8_t*>(h->d_stage[idx]), dst, st);
 }
 
 cudaError_t prof_mark(qmiv_handle* h, const char* name, cudaStream_t st, bool begin)
@@ -426,11 +489,26 @@ qmiv_status ensure_tmaps(qmiv_handle* h, DevJob& j, const CpsVariant& v, cudaStr
   key[9] = ((uint64_t)(uint32_t)j.W << 32) | (uint32_t)j.H;
   key[10] = ((uint64_t)RW << 48) | ((uint64_t)TH << 32) | ((uint64_t)CRW << 16) | CTH;
   key[11] = (uint64_t)sb;
-  j.tmaps = S.d_tmaps;
-  if(S.tmap_valid && std::memcmp(key, S.tmap_key, sizeof(key)) == 0) return QMIV_OK;
+  int e = -1, victim = 0;
+  for(int t = 0; t < Slot::kTmapSets; t++)
+  {
+    if(S.tmap_valid[t] && std::memcmp(key, S.tmap_key[t], sizeof(key)) == 0) { e = t; break; }
+    if(!S.tmap_valid[victim]) continue;
+    if(!S.tmap_valid[t] || S.tmap_stamp[t] < S.tmap_stamp[victim]) victim = t;
+  }
+  S.tmap_stamp[e >= 0 ? e : victim] = ++h->tmap_clock;
+  if(e >= 0) { j.tmaps = S.d_tmaps + (size_t)e * 6 * sizeof(CUtensorMap); return QMIV_OK; }
+  // a new layout replaces the least recently used set; the copy is stream-ordered after every
+  // earlier launch of the handle, so no kernel still reads the set it overwrites
+  e = victim;
+  j.tmaps = S.d_tmaps + (size_t)e * 6 * sizeof(CUtensorMap);
   EncodeTiledFn enc = encode_fn();
   if(!enc) return fail(QMIV_CUDA_ERROR, "cuTensorMapEncodeTiled unavailable");
-  alignas(64) CUtensorMap maps[6];
+  const int nr = (int)h->tmap_ev.size();
+  const int k = h->tmap_next;
+  h->tmap_next = (k + 1) % nr;
+  if(h->tmap_used[k]) CUDA_TRY(cudaEventSynchronize(h->tmap_ev[k]));
+  CUtensorMap* maps = reinterpret_cast<CUtensorMap*>(h->h_tmaps + (size_t)k * 6 * sizeof(CUtensorMap));
   for(int pic = 0; pic < 2; pic++)
     for(int c = 0; c < 3; c++)
     {
@@ -443,12 +521,14 @@ qmiv_status ensure_tmaps(qmiv_handle* h, DevJob& j, const CpsVariant& v, cudaStr
       CUresult r = enc(&maps[pic * 3 + c], sb == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 2,
                        const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-      if(r != CUDA_SUCCESS) { S.tmap_valid = false; return fail(QMIV_CUDA_ERROR, "cuTensorMapEncodeTiled failed (%d)", (int)r); }
+      if(r != CUDA_SUCCESS) { S.tmap_valid[e] = false; return fail(QMIV_CUDA_ERROR, "cuTensorMapEncodeTiled failed (%d)", (int)r); }
     }
-  CUDA_TRY(cudaMemcpyAsync(S.d_tmaps, maps, sizeof(maps), cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaStreamSynchronize(st)); // `maps` lives on this stack frame
-  std::memcpy(S.tmap_key, key, sizeof(key));
-  S.tmap_valid = true;
+  CUDA_TRY(cudaMemcpyAsync(S.d_tmaps + (size_t)e * 6 * sizeof(CUtensorMap), maps, 6 * sizeof(CUtensorMap),
+                           cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaEventRecord(h->tmap_ev[k], st));
+  h->tmap_used[k] = 1;
+  std::memcpy(S.tmap_key[e], key, sizeof(key));
+  S.tmap_valid[e] = true;
   return QMIV_OK;
 }
 
@@ -587,7 +667,8 @@ qmiv_status upload_tables(qmiv_handle* h, cudaStream_t st)
   if(h->tab_used[k]) CUDA_TRY(cudaEventSynchronize(h->tab_ev[k]));
   const size_t pos = pack_tables(h, h->h_tab[k], t.bytes);
   if(!pos) return fail(QMIV_TOO_LARGE, "call tables exceed %zu B", t.bytes);
-  CUDA_TRY(cudaMemcpyAsync(h->d_tab, h->h_tab[k], pos, cudaMemcpyHostToDevice, st));
+  CUDA_TRY(launch_copy_table(h->h_tab_dev[k], h->d_tab, pos, st));
+  h->launches++;
   CUDA_TRY(cudaEventRecord(h->tab_ev[k], st));
   h->tab_used[k] = true;
   return QMIV_OK;
@@ -654,6 +735,8 @@ qmiv_status launch_jobs(qmiv_handle* h, const LaunchPlan& P, const uint8_t* d_ta
   const int n = (int)h->jobs.size();
   const DevJob* d_jobs = reinterpret_cast<const DevJob*>(d_tab);
   h->prof_n = 0;
+  CUDA_TRY(launch_init_results(d_jobs, n, st));
+  h->launches++;
   if(P.any_stats)
   {
     CUDA_TRY(prof_mark(h, "k_stats", st, true));
@@ -829,7 +912,7 @@ qmiv_status qmiv_create(qmiv_handle** out, const qmiv_options* opt, int32_t max_
   const size_t rows_b = align256((size_t)max_h * 6 * sizeof(int64_t));
   const size_t cps_b = align256((size_t)2 * max_h * 3 * sizeof(unsigned long long));
   const size_t sc_b = align256(sizeof(JobScalars));
-  const size_t tm_b = align256(6 * 128);
+  const size_t tm_b = align256((size_t)Slot::kTmapSets * 6 * 128);
   const size_t per = rows_b + cps_b + sc_b + tm_b;
   if(cudaMalloc(&h->slot_mem, per * max_jobs) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "slot scratch %zu B", per * max_jobs));
   if(cudaMemset(h->slot_mem, 0, per * max_jobs) != cudaSuccess) return cleanup(fail(QMIV_CUDA_ERROR, "memset"));
@@ -842,6 +925,7 @@ qmiv_status qmiv_create(qmiv_handle** out, const qmiv_options* opt, int32_t max_
     h->slots[i].sc = (JobScalars*)b; b += sc_b;
     h->slots[i].d_tmaps = b;
   }
+  h->tmap_clock = 0;
   // per-slot scratch of the SSIM family, for the metrics the caller reserves
   const uint32_t sm = opt->scratch_metrics;
   size_t scp_b = 0, pyr_b = 0, part_floats = 0;
@@ -883,13 +967,23 @@ qmiv_status qmiv_create(qmiv_handle** out, const qmiv_options* opt, int32_t max_
   if(cudaMalloc(&h->d_tab, t.bytes) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "call tables"));
   for(int k = 0; k < qmiv_handle::kRing; k++)
   {
-    if(cudaMallocHost(&h->h_tab[k], t.bytes) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "pinned call tables"));
+    if(cudaHostAlloc((void**)&h->h_tab[k], t.bytes, cudaHostAllocMapped) != cudaSuccess ||
+       cudaHostGetDevicePointer((void**)&h->h_tab_dev[k], h->h_tab[k], 0) != cudaSuccess)
+      return cleanup(fail(QMIV_OUT_OF_MEMORY, "pinned call tables"));
     if(cudaEventCreateWithFlags(&h->tab_ev[k], cudaEventDisableTiming) != cudaSuccess) return cleanup(fail(QMIV_CUDA_ERROR, "event"));
   }
   for(int i = 0; i < 2; i++)
   { // staging for host pictures: up to 3 full planes of 16-bit samples with 16-byte row pitch
-    const size_t e = (size_t)((max_w + 7) & ~7) * max_h * 3 + 64;
+    const size_t e = (size_t)((max_w + 7) & ~7) * max_h * 3 + 512;
     if(cudaMalloc(&h->d_stage[i], e * sizeof(uint16_t)) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "staging"));
+  }
+  {
+    const int nr = 2 * max_jobs + 4;
+    if(cudaMallocHost(&h->h_tmaps, (size_t)nr * 6 * sizeof(CUtensorMap)) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "pinned tensor maps"));
+    h->tmap_ev.assign(nr, nullptr);
+    h->tmap_used.assign(nr, 0);
+    for(int k = 0; k < nr; k++)
+      if(cudaEventCreateWithFlags(&h->tmap_ev[k], cudaEventDisableTiming) != cudaSuccess) return cleanup(fail(QMIV_CUDA_ERROR, "event"));
   }
   if(cudaMalloc(&h->mask_rows, sizeof(int64_t) * kMaskRowVals * max_h) != cudaSuccess ||
      cudaMalloc(&h->mask_small, 256) != cudaSuccess || cudaMemset(h->mask_small, 0, 256) != cudaSuccess ||
@@ -910,6 +1004,16 @@ qmiv_status qmiv_destroy(qmiv_handle* h)
   cudaFree(h->d_tab);
   for(int k = 0; k < qmiv_handle::kRing; k++) { cudaFreeHost(h->h_tab[k]); if(h->tab_ev[k]) cudaEventDestroy(h->tab_ev[k]); }
   for(int i = 0; i < 2; i++) cudaFree(h->d_stage[i]);
+  if(h->up_stream) cudaStreamSynchronize(h->up_stream);
+  for(int i = 0; i < 2; i++)
+  {
+    cudaFree(h->d_up[i]);
+    if(h->up_done[i]) cudaEventDestroy(h->up_done[i]);
+    if(h->up_free[i]) cudaEventDestroy(h->up_free[i]);
+  }
+  if(h->up_stream) cudaStreamDestroy(h->up_stream);
+  for(auto e : h->tmap_ev) if(e) cudaEventDestroy(e);
+  cudaFreeHost(h->h_tmaps);
   cudaFree(h->mask_rows);
   cudaFree(h->mask_small);
   cudaFree(h->mask_stage);
@@ -1242,6 +1346,111 @@ qmiv_status qmiv_calc_batch(qmiv_handle* h, const qmiv_job* jobs, int32_t n, qmi
   qmiv_status s = fill_batch(h, jobs, n, results);
   if(s != QMIV_OK) return s;
   return run_jobs(h, (cudaStream_t)stream);
+}
+
+// ---- a batch of host pictures, uploaded in groups overlapped with the measurement ------------
+qmiv_status qmiv_calc_batch_host(qmiv_handle* h, const qmiv_job* jobs, int32_t n, qmiv_frame_result* results,
+                                 size_t group_bytes, qmiv_stream stream)
+{
+  if(!h) return fail(QMIV_BAD_ARG, "handle is null");
+  if(!jobs || n < 1) return fail(QMIV_BAD_ARG, "no jobs");
+  if(!results) return fail(QMIV_BAD_ARG, "results is null");
+  const cudaStream_t st = (cudaStream_t)stream;
+  std::vector<size_t> bytes(n);
+  size_t largest = 0, total = 0;
+  for(int i = 0; i < n; i++)
+  {
+    qmiv_status s = check_pair(h, &jobs[i].pic0, &jobs[i].pic1);
+    if(s != QMIV_OK) return fail(s, "job %d: %s", i, g_last_error.c_str());
+    if(jobs[i].pic0.is_device) return fail(QMIV_BAD_ARG, "job %d: qmiv_calc_batch_host takes host pictures", i);
+    bytes[i] = stage_bytes(&jobs[i].pic0) + stage_bytes(&jobs[i].pic1);
+    largest = std::max(largest, bytes[i]);
+    total += bytes[i];
+  }
+  const bool taper = group_bytes == 0;
+  if(group_bytes == 0) group_bytes = (total + 15) / 16;
+  group_bytes = std::max(group_bytes, largest);
+  // consecutive jobs per group, bounded by group_bytes and max_jobs. With the default size the
+  // last two group sizes' worth of pictures go in quarter-size groups: the measurement of the
+  // last group is the one part that no upload hides.
+  std::vector<int> first(1, 0);
+  {
+    size_t acc = 0, done = 0, budget = group_bytes;
+    for(int i = 0; i < n; i++)
+    {
+      if(i > first.back() && (acc + bytes[i] > budget || i - first.back() >= h->max_jobs))
+      {
+        first.push_back(i);
+        done += acc;
+        acc = 0;
+        if(taper && total - done <= 2 * group_bytes) budget = std::max(largest, group_bytes / 4);
+      }
+      acc += bytes[i];
+    }
+  }
+  first.push_back(n);
+  const int groups = (int)first.size() - 1;
+  if(!h->up_stream)
+  {
+    CUDA_TRY(cudaStreamCreateWithFlags(&h->up_stream, cudaStreamNonBlocking));
+    for(int i = 0; i < 2; i++)
+    {
+      CUDA_TRY(cudaEventCreateWithFlags(&h->up_done[i], cudaEventDisableTiming));
+      CUDA_TRY(cudaEventCreateWithFlags(&h->up_free[i], cudaEventDisableTiming));
+    }
+  }
+  size_t need = 0;
+  for(int g = 0; g < groups; g++)
+  {
+    size_t b = 0;
+    for(int i = first[g]; i < first[g + 1]; i++) b += bytes[i];
+    need = std::max(need, b);
+  }
+  if(need > h->up_cap)
+  { // grow: earlier work on either buffer must have finished
+    CUDA_TRY(cudaStreamSynchronize(h->up_stream));
+    CUDA_TRY(cudaStreamSynchronize(st));
+    for(int i = 0; i < 2; i++)
+    {
+      cudaFree(h->d_up[i]);
+      h->d_up[i] = nullptr;
+      h->up_recorded[i] = false;
+    }
+    h->up_cap = 0;
+    for(int i = 0; i < 2; i++)
+      if(cudaMalloc(&h->d_up[i], need) != cudaSuccess) return fail(QMIV_OUT_OF_MEMORY, "host-batch group buffers 2 x %zu B", need);
+    h->up_cap = need;
+  }
+  std::vector<std::vector<qmiv_job>> staged(groups);
+  auto upload = [&](int g) -> qmiv_status {
+    const int b = g & 1;
+    if(h->up_recorded[b]) CUDA_TRY(cudaStreamWaitEvent(h->up_stream, h->up_free[b], 0));
+    size_t off = 0;
+    staged[g].assign(jobs + first[g], jobs + first[g + 1]);
+    for(int i = first[g]; i < first[g + 1]; i++)
+    {
+      qmiv_job& d = staged[g][i - first[g]];
+      qmiv_status s = stage_pic(&jobs[i].pic0, h->d_up[b] + off, &d.pic0, h->up_stream);
+      if(s != QMIV_OK) return s;
+      off += stage_bytes(&jobs[i].pic0);
+      if((s = stage_pic(&jobs[i].pic1, h->d_up[b] + off, &d.pic1, h->up_stream)) != QMIV_OK) return s;
+      off += stage_bytes(&jobs[i].pic1);
+    }
+    CUDA_TRY(cudaEventRecord(h->up_done[b], h->up_stream));
+    return QMIV_OK;
+  };
+  qmiv_status s = upload(0);
+  for(int g = 0; g < groups && s == QMIV_OK; g++)
+  {
+    if(g + 1 < groups && (s = upload(g + 1)) != QMIV_OK) break;  // the next group uploads while this one runs
+    const int b = g & 1;
+    CUDA_TRY(cudaStreamWaitEvent(st, h->up_done[b], 0));
+    if((s = fill_batch(h, staged[g].data(), first[g + 1] - first[g], results + first[g])) != QMIV_OK) break;
+    if((s = run_jobs(h, st)) != QMIV_OK) break;
+    CUDA_TRY(cudaEventRecord(h->up_free[b], st));
+    h->up_recorded[b] = true;
+  }
+  return s;
 }
 
 // ---- a batch captured once as a CUDA graph ----------------------------------------------------

@@ -61,6 +61,8 @@ struct Params {
 };
 
 // Host-side launchers (defined in the .cu files).
+cudaError_t launch_init_results(const DevJob* d_jobs, int n, cudaStream_t st);
+cudaError_t launch_copy_table(const void* src, void* dst, size_t bytes, cudaStream_t st);  // bytes: a multiple of 16
 cudaError_t launch_stats(const DevJob* d_jobs, const DevJob* h_jobs, int n, const Params& p, cudaStream_t st);
 
 // Statistics of one picture pair in a static device array (k_stats.cu): no allocation.
