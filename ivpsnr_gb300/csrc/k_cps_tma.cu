@@ -16,6 +16,7 @@
 //     component and accumulated in shared memory, then added to the job's row sums.
 #include <climits>
 #include <cstdio>
+#include <type_traits>
 
 #include "qmiv_cps_common.cuh"
 #include "qmiv_ptx.cuh"
@@ -26,9 +27,11 @@ namespace {
 
 constexpr uint32_t kWaitPolls = 1u << 22;
 
-template <int SR, int QPW, int NWD, typename T>
+template <int SR, int QPW, int NWD, typename T, typename KeyT>
 struct TGeo {
   static constexpr int SB   = (int)sizeof(T);
+  // ints per converted luma sample: (s*v, (s*v)^2) for the 32-bit expanded-key search
+  static constexpr int CE   = sizeof(KeyT) == 4 ? 2 : 1;
   static constexpr int R    = 2 * QPW * NWD;                   // strip rows
   static constexpr int NT   = 64 * NWD;                        // threads (2 directions x NWD warps)
   static constexpr int XA   = 16 / SB;                         // box x alignment in samples
@@ -45,19 +48,22 @@ struct TGeo {
   static constexpr int CBOX = (CTH * CRW * SB + 127) / 128 * 128;
   static constexpr int STAGE = 2 * LBOX + 4 * CBOX;
   static constexpr uint32_t TX = 2u * TH * RW * SB + 4u * CTH * CRW * SB;
-  static constexpr int CVT  = 2 * TH * TW * 4;
+  static constexpr int CVT  = 2 * TH * TW * 4 * CE;
   static constexpr int ACC  = 2 * R * 3 * 8;
   static constexpr int SMEM = 2 * STAGE + CVT + ACC + 16;
+  // resident blocks the register budget is sized for: 24 warps per SM at search range <= 2
+  static constexpr int MINB = SR <= 2 ? 768 / NT : 512 / NT;
   static_assert(SR <= XA, "halo wider than the box alignment pad");
   static_assert(RW <= 256 && TH <= 256 && CRW <= 256 && CTH <= 256, "tensor box too large");
 };
 
 template <int SR, int QPW, int NWD, typename KeyT, typename T>
-__global__ void __launch_bounds__(TGeo<SR, QPW, NWD, T>::NT)
+__global__ void __launch_bounds__(TGeo<SR, QPW, NWD, T, KeyT>::NT, TGeo<SR, QPW, NWD, T, KeyT>::MINB)
 k_cps420_tma(const DevJob* __restrict__ jobs, int njobs, Params p)
 {
-  using G = TGeo<SR, QPW, NWD, T>;
+  using G = TGeo<SR, QPW, NWD, T, KeyT>;
   constexpr int W2 = 2 * SR + 1;
+  constexpr int CE = G::CE;
   extern __shared__ __align__(128) unsigned char smem[];
   int* cvt = reinterpret_cast<int*>(smem + 2 * G::STAGE);
   unsigned long long* acc = reinterpret_cast<unsigned long long*>(smem + 2 * G::STAGE + G::CVT);
@@ -147,15 +153,17 @@ k_cps420_tma(const DevJob* __restrict__ jobs, int njobs, Params p)
           const int x1 = clampi(cx0 - SR + tx + 1, 0, W - 1) - (cx0 - G::XA);
           v0 = rl[ry * G::RW + x0]; v1 = rl[ry * G::RW + x1];
         }
-        *reinterpret_cast<int2*>(&cvt[(pic * G::TH + ty) * G::TW + tx]) = make_int2(s * v0, s * v1);
+        const int e = (pic * G::TH + ty) * G::TW + tx;
+        if constexpr(CE == 2) *reinterpret_cast<int4*>(&cvt[2 * e]) = make_int4(s * v0, s * v0 * s * v0, s * v1, s * v1 * s * v1);
+        else                  *reinterpret_cast<int2*>(&cvt[e]) = make_int2(s * v0, s * v1);
       }
     }
     __syncthreads();
 
     // ---- search ----
     {
-      const int* cvtT = cvt + tp * G::TH * G::TW;
-      const int* cvtR = cvt + rp * G::TH * G::TW;
+      const int* cvtT = cvt + tp * G::TH * G::TW * CE;
+      const int* cvtR = cvt + rp * G::TH * G::TW * CE;
       const T* chrT0 = reinterpret_cast<const T*>(sb + 2 * G::LBOX + (tp * 2 + 0) * G::CBOX);
       const T* chrT1 = reinterpret_cast<const T*>(sb + 2 * G::LBOX + (tp * 2 + 1) * G::CBOX);
       const T* chrR0 = reinterpret_cast<const T*>(sb + 2 * G::LBOX + (rp * 2 + 0) * G::CBOX);
@@ -166,6 +174,11 @@ k_cps420_tma(const DevJob* __restrict__ jobs, int njobs, Params p)
       for(int j = 0; j < G::NC; j++) ccol[j] = clampi(cxh + lane - G::CS + j, 0, Wc - 1) - crx0;
       const int tcol = clampi(cxh + lane, 0, Wc - 1) - crx0;
 
+      // Chunks whose search windows, chroma cells and pixels all lie inside the picture skip
+      // every clamp and validity mask (IN = true); the edge chunks keep them.
+      const bool interior = y0 >= 2 * SR + 2 && y0 + G::R + 2 * SR + 2 <= H && cx0 >= 2 * SR + 2 && cx0 + 64 + 2 * SR + 2 <= W;
+      auto run_quads = [&](auto in_tag) {
+      constexpr bool IN = decltype(in_tag)::value;
       #pragma unroll 1
       for(int qi = 0; qi < QPW; qi++)
       {
@@ -176,20 +189,29 @@ k_cps420_tma(const DevJob* __restrict__ jobs, int njobs, Params p)
         #pragma unroll
         for(int a = 0; a < 2; a++)
         {
-          const int2 v = *reinterpret_cast<const int2*>(&cvtT[(2 * qr + a + SR) * G::TW + 2 * lane + SR - (SR & 1)]);
-          if(SR & 1) { tY[a][0] = v.y; tY[a][1] = cvtT[(2 * qr + a + SR) * G::TW + 2 * lane + SR + 1]; }
-          else       { tY[a][0] = v.x; tY[a][1] = v.y; }
+          const int e = (2 * qr + a + SR) * G::TW + 2 * lane + SR;
+          if constexpr(CE == 2)
+          {
+            if(SR & 1) { tY[a][0] = cvtT[2 * e]; tY[a][1] = cvtT[2 * e + 2]; }
+            else       { const int4 v = *reinterpret_cast<const int4*>(&cvtT[2 * e]); tY[a][0] = v.x; tY[a][1] = v.z; }
+          }
+          else
+          {
+            const int2 v = *reinterpret_cast<const int2*>(&cvtT[e - (SR & 1)]);
+            if(SR & 1) { tY[a][0] = v.y; tY[a][1] = cvtT[e + 1]; }
+            else       { tY[a][0] = v.x; tY[a][1] = v.y; }
+          }
           tY[a][0] += s * gd0; tY[a][1] += s * gd0;
         }
         const int qc = (y0 >> 1) + qr;
-        const int trow = clampi(qc, 0, Hc - 1) - cry0;
+        const int trow = (IN ? qc : clampi(qc, 0, Hc - 1)) - cry0;
         const int tCb = (int)chrT0[trow * G::CRW + tcol] + gd1;
         const int tCr = (int)chrT1[trow * G::CRW + tcol] + gd2;
         KeyT B[G::NC][G::NC];
         #pragma unroll
         for(int jr = 0; jr < G::NC; jr++)
         {
-          const int crow = clampi(qc - G::CS + jr, 0, Hc - 1) - cry0;
+          const int crow = (IN ? qc - G::CS + jr : clampi(qc - G::CS + jr, 0, Hc - 1)) - cry0;
           #pragma unroll
           for(int jc = 0; jc < G::NC; jc++)
           {
@@ -199,70 +221,137 @@ k_cps420_tma(const DevJob* __restrict__ jobs, int njobs, Params p)
           }
         }
         KeyT best[2][2];
-        best[0][0] = best[0][1] = best[1][0] = best[1][1] = (KeyT)~(KeyT)0;
-        #pragma unroll
-        for(int rr = 0; rr < 2 * SR + 2; rr++)
+        if constexpr(sizeof(KeyT) == 4)
         {
-          int r[2 * SR + 2];
-          const int* lrow = cvtR + (2 * qr + rr) * G::TW + 2 * lane;
-          #pragma unroll
-          for(int jj = 0; jj < SR + 1; jj++) { const int2 v = *reinterpret_cast<const int2*>(lrow + 2 * jj); r[2 * jj] = v.x; r[2 * jj + 1] = v.y; }
-          const int jr = fdiv2(rr - SR) + G::CS;
+          // Expanded key. With TY the scaled tested luma, R a reference luma sample and B its
+          // chroma cost, key(k) = (TY - R)^2 + B + k = TY^2 - 2 TY R + (R^2 + B + k). TY^2 is
+          // constant per pixel, and so is the offset between the window index k and the
+          // tile position kk = rr*KS + j of R (k = kk - (a*KS + px)), while B depends on R's
+          // position only (its chroma cell). So per reference position z = R^2 + B + kk is
+          // formed once for all four pixels of the quad, and each candidate is one
+          // multiply-add (-2 TY) * R + z and a share of a three-way minimum. The candidates
+          // of a pixel lie in [-TY^2 + c, kmax - TY^2 + c], inside int32 whenever the packed
+          // key is below 2^31 (the host picks these variants only then), so wrapping
+          // 32-bit arithmetic gives their exact values; the packed key is recovered by
+          // adding TY^2 - c back.
+          int nt[2][2], bs[2][2];
           #pragma unroll
           for(int a = 0; a < 2; a++)
+            #pragma unroll
+            for(int px = 0; px < 2; px++) { nt[a][px] = -2 * tY[a][px]; bs[a][px] = INT_MAX; }
+          #pragma unroll
+          for(int rr = 0; rr < 2 * SR + 2; rr++)
           {
-            const int dy = rr - SR - a;
-            if(dy < -SR || dy > SR) continue;
+            int r[2 * SR + 2];
+            unsigned z[2 * SR + 2];
+            const int* lrow = cvtR + ((2 * qr + rr) * G::TW + 2 * lane) * 2;
+            const int jr = fdiv2(rr - SR) + G::CS;
+            #pragma unroll
+            for(int jj = 0; jj < SR + 1; jj++)
+            {
+              const int4 v = *reinterpret_cast<const int4*>(lrow + 4 * jj);
+              r[2 * jj] = v.x; z[2 * jj] = (unsigned)v.y;
+              r[2 * jj + 1] = v.z; z[2 * jj + 1] = (unsigned)v.w;
+            }
+            #pragma unroll
+            for(int j = 0; j < 2 * SR + 2; j++) z[j] += (unsigned)B[jr][fdiv2(j - SR) + G::CS] + (unsigned)(rr * G::KS + j);
+            #pragma unroll
+            for(int a = 0; a < 2; a++)
+            {
+              const int dy = rr - SR - a;
+              if(dy < -SR || dy > SR) continue;
+              #pragma unroll
+              for(int px = 0; px < 2; px++)
+                #pragma unroll
+                for(int dx = -SR; dx <= SR; dx++)
+                {
+                  const int j = px + dx + SR;
+                  bs[a][px] = min(bs[a][px], (int)((unsigned)nt[a][px] * (unsigned)r[j] + z[j]));
+                }
+            }
+          }
+          #pragma unroll
+          for(int a = 0; a < 2; a++)
             #pragma unroll
             for(int px = 0; px < 2; px++)
+              best[a][px] = (KeyT)((unsigned)bs[a][px] + (unsigned)tY[a][px] * (unsigned)tY[a][px] - (unsigned)(a * G::KS + px));
+        }
+        else
+        {
+          best[0][0] = best[0][1] = best[1][0] = best[1][1] = (KeyT)~(KeyT)0;
+          #pragma unroll
+          for(int rr = 0; rr < 2 * SR + 2; rr++)
+          {
+            int r[2 * SR + 2];
+            const int* lrow = cvtR + (2 * qr + rr) * G::TW + 2 * lane;
+            #pragma unroll
+            for(int jj = 0; jj < SR + 1; jj++) { const int2 v = *reinterpret_cast<const int2*>(lrow + 2 * jj); r[2 * jj] = v.x; r[2 * jj + 1] = v.y; }
+            const int jr = fdiv2(rr - SR) + G::CS;
+            #pragma unroll
+            for(int a = 0; a < 2; a++)
+            {
+              const int dy = rr - SR - a;
+              if(dy < -SR || dy > SR) continue;
               #pragma unroll
-              for(int dx = -SR; dx <= SR; dx++)
-              {
-                // window index with a power-of-two row pitch: same order as the row-major scan
-                const int k = (dy + SR) * G::KS + (dx + SR);
-                const int jc = fdiv2(px + dx) + G::CS;
-                const int dd = tY[a][px] - r[px + dx + SR];
-                // (dd^2 + chroma) is one multiply-add; "+ k, min" fuses into one add-min
-                if(sizeof(KeyT) == 4)
+              for(int px = 0; px < 2; px++)
+                #pragma unroll
+                for(int dx = -SR; dx <= SR; dx++)
                 {
-                  const unsigned t = (unsigned)(dd * dd) + (unsigned)B[jr][jc];
-                  best[a][px] = min((unsigned)best[a][px], t + (unsigned)k);
+                  // window index with a power-of-two row pitch: same order as the row-major scan
+                  const int k = (dy + SR) * G::KS + (dx + SR);
+                  const int jc = fdiv2(px + dx) + G::CS;
+                  const int dd = tY[a][px] - r[px + dx + SR];
+                  best[a][px] = min(best[a][px], (KeyT)((long long)dd * dd) + B[jr][jc] + (KeyT)k);
                 }
-                else best[a][px] = min(best[a][px], (KeyT)((long long)dd * dd) + B[jr][jc] + (KeyT)k);
-              }
+            }
           }
         }
 
         // argmin: exact per-component squared error, SCP samples
         unsigned sq[2][3] = { { 0, 0, 0 }, { 0, 0, 0 } };
+        int sv[2][2][3];
         #pragma unroll
         for(int a = 0; a < 2; a++)
           #pragma unroll
           for(int px = 0; px < 2; px++)
           {
-            const int y = yq + a, x = cx0 + 2 * lane + px;
-            const bool valid = y < H && x < W;
             const unsigned k = p.key_m_log2 >= 0 ? (unsigned)(best[a][px] & (KeyT)(p.key_m - 1))
                                                  : (unsigned)(best[a][px] % (KeyT)p.key_m);
             const int dy = (int)(k >> G::KS_LOG2) - SR, dx = (int)(k & (G::KS - 1)) - SR;
-            const int rl = cvtR[(2 * qr + a + SR + dy) * G::TW + 2 * lane + px + SR + dx];
-            const int crow = clampi(qc + ((a + dy) >> 1), 0, Hc - 1) - cry0;
-            const int ccl = clampi(cxh + lane + ((px + dx) >> 1), 0, Wc - 1) - crx0;
+            const int rl = cvtR[((2 * qr + a + SR + dy) * G::TW + 2 * lane + px + SR + dx) * CE];
+            const int crow = (IN ? qc + ((a + dy) >> 1) : clampi(qc + ((a + dy) >> 1), 0, Hc - 1)) - cry0;
+            const int ccl = (IN ? cxh + lane + ((px + dx) >> 1) : clampi(cxh + lane + ((px + dx) >> 1), 0, Wc - 1)) - crx0;
             const int rcb = chrR0[crow * G::CRW + ccl], rcr = chrR1[crow * G::CRW + ccl];
             int rY, tYr;
             if(p.luma_scale_log2 >= 0) { rY = rl >> p.luma_scale_log2; tYr = tY[a][px] >> p.luma_scale_log2; }
             else                       { rY = rl / s; tYr = tY[a][px] / s; }
             const int d0 = tYr - rY, d1 = tCb - rcb, d2 = tCr - rcr;
-            const unsigned vm = valid ? 0xFFFFFFFFu : 0u;
-            sq[a][0] += (unsigned)(d0 * d0) & vm; sq[a][1] += (unsigned)(d1 * d1) & vm; sq[a][2] += (unsigned)(d2 * d2) & vm;
-            if(want_scp && valid)
-            { // clipU(ref - GCD) (xShftCompPic.cpp:88-92); for T2R the shift is -GCD
-              const int64_t o = (int64_t)y * J.scp_stride + x;
-              scp[0][o] = (uint16_t)clampi(rY - gd0, 0, mx);
-              scp[1][o] = (uint16_t)clampi(rcb - gd1, 0, mx);
-              scp[2][o] = (uint16_t)clampi(rcr - gd2, 0, mx);
+            if(IN)
+            {
+              sq[a][0] += (unsigned)(d0 * d0); sq[a][1] += (unsigned)(d1 * d1); sq[a][2] += (unsigned)(d2 * d2);
             }
+            else
+            {
+              const unsigned vm = (yq + a < H && cx0 + 2 * lane + px < W) ? 0xFFFFFFFFu : 0u;
+              sq[a][0] += (unsigned)(d0 * d0) & vm; sq[a][1] += (unsigned)(d1 * d1) & vm; sq[a][2] += (unsigned)(d2 * d2) & vm;
+            }
+            sv[a][px][0] = rY; sv[a][px][1] = rcb; sv[a][px][2] = rcr;
           }
+        if(want_scp)
+        { // clipU(ref - GCD) (xShftCompPic.cpp:88-92); for T2R the shift is -GCD
+          #pragma unroll
+          for(int a = 0; a < 2; a++)
+            #pragma unroll
+            for(int px = 0; px < 2; px++)
+            {
+              const int y = yq + a, x = cx0 + 2 * lane + px;
+              if(!IN && !(y < H && x < W)) continue;
+              const int64_t o = (int64_t)y * J.scp_stride + x;
+              scp[0][o] = (uint16_t)clampi(sv[a][px][0] - gd0, 0, mx);
+              scp[1][o] = (uint16_t)clampi(sv[a][px][1] - gd1, 0, mx);
+              scp[2][o] = (uint16_t)clampi(sv[a][px][2] - gd2, 0, mx);
+            }
+        }
         #pragma unroll
         for(int a = 0; a < 2; a++)
           #pragma unroll
@@ -275,6 +364,9 @@ k_cps420_tma(const DevJob* __restrict__ jobs, int njobs, Params p)
             if(lane == 0) acc[(dir * G::R + 2 * qr + a) * 3 + c] += v;
           }
       }
+      };
+      if(interior) run_quads(std::true_type{});
+      else         run_quads(std::false_type{});
     }
     __syncthreads();
   }
@@ -300,11 +392,15 @@ k_cps420_tma(const DevJob* __restrict__ jobs, int njobs, Params p)
 template <int SR, int QPW, int NWD, typename KeyT, typename T>
 cudaError_t launch_tma(const DevJob* d, int n, int blocks, const Params& p, cudaStream_t st)
 {
-  using G = TGeo<SR, QPW, NWD, T>;
+  using G = TGeo<SR, QPW, NWD, T, KeyT>;
   static bool attr = false;
   if(!attr)
   {
     cudaError_t e = cudaFuncSetAttribute(k_cps420_tma<SR, QPW, NWD, KeyT, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM);
+    if(e != cudaSuccess) return e;
+    // all of the unified L1 as shared memory: the kernel stages through TMA and reads no
+    // global data through L1, and the default split held it to two resident blocks
+    e = cudaFuncSetAttribute(k_cps420_tma<SR, QPW, NWD, KeyT, T>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if(e != cudaSuccess) return e;
     attr = true;
   }

@@ -205,7 +205,9 @@ void derive_params(qmiv_handle* h)
   p.one = 1;
 }
 
-// Does the 32-bit packed key hold for this bit depth?
+// Does the 32-bit packed key hold for this bit depth? The 32-bit TMA search evaluates keys
+// relative to the tested sample's square in signed 32-bit arithmetic, so the key must stay
+// below 2^31 (with room for the window-index offset) and the scaled samples' squares too.
 bool key32_ok(const qmiv_handle* h, int bd)
 {
   const Params& p = h->params;
@@ -215,7 +217,7 @@ bool key32_ok(const qmiv_handle* h, int bd)
   const uint64_t wsum = (uint64_t)p.w_search[0] + p.w_search[1] + p.w_search[2];
   const uint64_t N = window_index_bound(p.sr);
   const uint64_t kmax = (uint64_t)p.key_m * wsum * D * D + N;
-  return kmax < (1ull << 32) && (uint64_t)p.luma_scale * D < 46340ull;
+  return kmax + 64 < (1ull << 31) && (uint64_t)p.luma_scale * D < 46340ull;
 }
 
 // Can the TMA kernels stage this job? 16-byte aligned planes and row pitches.
