@@ -21,6 +21,7 @@
 #include <cfloat>
 
 #include "qmiv_device.cuh"
+#include "qmiv_ptx.cuh"
 #include "qmiv_ssim.h"
 
 namespace qmiv {
@@ -244,17 +245,46 @@ __global__ void __launch_bounds__(kThreads, 3) k_ssim(const SsimJob* __restrict_
 // moment streams (S1 of the four planes; S(a^2+b^2) and S(ab) of the three pairs (P0,P1),
 // (P0,SCP1), (P1,SCP0)) give SSIM, CS, IV-SSIM T2R and R2T, against sixteen for four separate
 // pair evaluations. Tiles are 16 rows high (the ten streams' vertical sums fill shared memory
-// faster); the staging is (P0, P1, SCP1, SCP0) float4 per sample, centred by the tile-centre
-// sample of P1.
+// faster).
+//
+// Staging: each tile needs one box per plane (the tile's rows and columns plus the window halo,
+// its left edge rounded down to 16 bytes; half-resolution boxes for 4:2:0 chroma, which the
+// vertical pass reads at (x >> 1, y >> 1)). Boxes are raw samples in two shared-memory stages:
+// one thread issues the four bulk-tensor loads of the next tile into the other stage while the
+// block works on the current one (mbarrier per stage, every wait bounded). Planes that a tensor
+// map cannot describe (unaligned base or pitch) are staged by the block itself with plain loads
+// into the same box layout, coordinates clamped at the picture edges; the bulk loads read zeros
+// there instead. Either way those samples feed only outputs outside the valid region. The
+// vertical pass converts samples to FP32 as it reads them: 2^23 + v is formed by its bit
+// pattern and (2^23 + tc) subtracted, exactly, which centres the tile on tc, the tile-centre
+// sample of picture 1.
 constexpr int kQTY = 16, kQPairs = 5;
+constexpr uint32_t kQuadPolls = 1u << 22;
 template <int WIN> struct QGeo {
   static constexpr int TX = kIW - WIN + 1;
   static constexpr int IH = kQTY + WIN - 1;
-  static constexpr int RPW = (IH + 7) / 8;
-  // staged [IH][64] float4; vertical sums [5][16][kRP] float2; row sums [4][7][16] float
-  static constexpr int SMEM = IH * kIW * 16 + kQPairs * kQTY * kRP * 8 + 4 * 7 * kQTY * 4;
-  static_assert(4 * 14 >= TX && 4 * 13 + 3 + WIN - 1 < kRP, "tile columns");
+  static constexpr int RP = WIN == 10 ? 65 : 67;                 // odd float2 pitch of the vertical sums
+  static constexpr int BH1 = (IH + 1) / 2 + 1;                   // box rows of a half-resolution plane
+  static constexpr int SLOT = ((64 + 8) * 2 * IH + 127) / 128 * 128;  // largest box: uint16, full resolution
+  static constexpr int STAGE = 4 * SLOT;
+  static constexpr int SV = kQPairs * kQTY * RP * 8;
+  static constexpr int RED = 4 * 7 * kQTY * 4;
+  static constexpr int SMEM = 2 * STAGE + SV + RED + 16;
+  static_assert(4 * 14 >= TX && 4 * 13 + 3 + WIN - 1 < RP, "tile columns");
 };
+}  // namespace
+int quad_box_h(int window, int shift) { const int ih = kQTY + (window == QMIV_SSIM_GAUSS11 ? 11 : 10) - 1; return shift ? (ih + 1) / 2 + 1 : ih; }
+namespace {
+
+__device__ __forceinline__ void fence_proxy_async_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Box origin of plane `pl` for the tile whose staged region starts at (xr, yr) = (x0-5, y0-5).
+__device__ __forceinline__ void quad_box_origin(const SsimPlane& pl, int xr, int yr, int& xs, int& ys)
+{
+  const int xa = 16 / pl.sbytes;
+  xs = (pl.shift ? xr >> 1 : xr) & ~(xa - 1);
+  ys = pl.shift ? yr >> 1 : yr;
+}
 
 __device__ __forceinline__ float ssim_index(float S1a, float S1b, float Sq, float Sx, float om2c, float omc,
                                             float k_cc, float cw0, float C1, float C2, bool calc_l)
@@ -272,14 +302,119 @@ __device__ __forceinline__ float ssim_index(float S1a, float S1b, float Sq, floa
   return __fdividef(num, den);
 }
 
+// One plane's column pointer for the vertical pass: even/odd staged-row bases (they differ for a
+// half-resolution plane whose first staged row is odd) and the row pitch in samples.
+template <typename T, int SH>
+struct QCol {
+  const T* e;
+  const T* o;
+  __device__ __forceinline__ QCol(const unsigned char* box, int bw, int xr, int yr, int xs, int q, int rg)
+  {
+    const T* b = reinterpret_cast<const T*>(box);
+    if(SH)
+    {
+      const int par = yr & 1, c = ((xr + q) >> 1) - xs;
+      e = b + 2 * rg * bw + c;
+      o = e + par * bw;
+    }
+    else
+    {
+      e = b + 4 * rg * bw + (xr - xs) + q;
+      o = e;
+    }
+  }
+  // staged row i (0 .. 3 + WIN - 1) of the thread's output-row group, compile-time i
+  template <int BW>
+  __device__ __forceinline__ unsigned at(int i) const
+  {
+    if(SH) return (i & 1) ? (unsigned)o[((i - 1) >> 1) * BW] : (unsigned)e[(i >> 1) * BW];
+    return (unsigned)e[i * BW];
+  }
+};
+
+// Vertical pass of a tile: thread = staged column q x output rows 4rg .. 4rg+3; five float2
+// stream pairs per output row into s_v.
+template <int WIN, typename T0, int SH0>
+__device__ __forceinline__ void quad_vpass(const unsigned char* stg, const SsimQuadJob& J, int xr, int yr, float tc,
+                                           const float2 (&gk)[WIN], float2* s_v, int q, int rg)
+{
+  using G = QGeo<WIN>;
+  constexpr int BW0 = quad_box_w((int)sizeof(T0), SH0), BWS = quad_box_w(2, 0);
+  int xs, ys;
+  quad_box_origin(J.p0, xr, yr, xs, ys);
+  const QCol<T0, SH0> c0(stg, BW0, xr, yr, xs, q, rg);
+  const QCol<T0, SH0> c1(stg + G::SLOT, BW0, xr, yr, xs, q, rg);
+  quad_box_origin(J.scp1, xr, yr, xs, ys);
+  const QCol<uint16_t, 0> c2(stg + 2 * G::SLOT, BWS, xr, yr, xs, q, rg);
+  const QCol<uint16_t, 0> c3(stg + 3 * G::SLOT, BWS, xr, yr, xs, q, rg);
+  const float2 mk = make_float2(-(8388608.0f + tc), -(8388608.0f + tc));
+  float2 acc[4][kQPairs];
+  #pragma unroll
+  for(int o = 0; o < 4; o++)
+    #pragma unroll
+    for(int m = 0; m < kQPairs; m++) acc[o][m] = make_float2(0.f, 0.f);
+  #pragma unroll
+  for(int i = 0; i < 3 + WIN; i++)
+  {
+    const float2 v01 = __fadd2_rn(make_float2(__uint_as_float(0x4B000000u | c0.template at<BW0>(i)),
+                                              __uint_as_float(0x4B000000u | c1.template at<BW0>(i))), mk);
+    const float2 v23 = __fadd2_rn(make_float2(__uint_as_float(0x4B000000u | c2.template at<BWS>(i)),
+                                              __uint_as_float(0x4B000000u | c3.template at<BWS>(i))), mk);
+    const float2 sq01 = __fmul2_rn(v01, v01);
+    const float2 sq23 = __fmul2_rn(v23, v23);
+    float2 st[kQPairs];
+    st[0] = v01;
+    st[1] = v23;
+    st[2] = make_float2(sq01.x + sq01.y, v01.x * v01.y);   // (P0, P1)
+    st[3] = make_float2(sq01.x + sq23.x, v01.x * v23.x);   // (P0, SCP1)
+    st[4] = make_float2(sq01.y + sq23.y, v01.y * v23.y);   // (P1, SCP0)
+    #pragma unroll
+    for(int o = 0; o < 4; o++)
+    {
+      const int k = i - o;
+      if(k < 0 || k >= WIN) continue;
+      #pragma unroll
+      for(int m = 0; m < kQPairs; m++) acc[o][m] = __ffma2_rn(gk[k], st[m], acc[o][m]);
+    }
+  }
+  #pragma unroll
+  for(int o = 0; o < 4; o++)
+    #pragma unroll
+    for(int m = 0; m < kQPairs; m++) s_v[(m * kQTY + 4 * rg + o) * G::RP + q] = acc[o][m];
+}
+
+// The boxes of a tile whose planes have no tensor maps, by plain loads with clamped coordinates.
+template <int WIN>
+__device__ __forceinline__ void quad_fill(unsigned char* stg, const SsimQuadJob& J, int xr, int yr)
+{
+  using G = QGeo<WIN>;
+  #pragma unroll
+  for(int p = 0; p < 4; p++)
+  {
+    const SsimPlane& P = p == 0 ? J.p0 : (p == 1 ? J.p1 : (p == 2 ? J.scp1 : J.scp0));
+    int xs, ys;
+    quad_box_origin(P, xr, yr, xs, ys);
+    const int bw = quad_box_w(P.sbytes, P.shift), bh = P.shift ? G::BH1 : G::IH;
+    const int wp = P.shift ? J.W >> 1 : J.W, hp = P.shift ? J.H >> 1 : J.H;
+    unsigned char* box = stg + p * G::SLOT;
+    for(int idx = threadIdx.x; idx < bw * bh; idx += kThreads)
+    {
+      const int r = idx / bw, c = idx - r * bw;
+      const int64_t o = (int64_t)min(ys + r, hp - 1) * P.stride + min(xs + c, wp - 1);
+      if(P.sbytes == 1) box[idx] = __ldg((const uint8_t*)P.ptr + o);
+      else reinterpret_cast<uint16_t*>(box)[idx] = __ldg((const uint16_t*)P.ptr + o);
+    }
+  }
+}
+
 template <int WIN>
 __global__ void __launch_bounds__(kThreads, 3) k_ssim_quad(const SsimQuadJob* __restrict__ jobs, int njobs, int ntiles)
 {
   using G = QGeo<WIN>;
-  extern __shared__ __align__(16) float smem[];
-  float4* s_in = reinterpret_cast<float4*>(smem);                                  // [IH][64]
-  float2* s_v = reinterpret_cast<float2*>(smem + 4 * G::IH * kIW);                // [5][16][kRP]
-  float* s_red = smem + 4 * G::IH * kIW + 2 * kQPairs * kQTY * kRP;               // [4][7][16]
+  extern __shared__ __align__(128) unsigned char qsm[];
+  float2* s_v = reinterpret_cast<float2*>(qsm + 2 * G::STAGE);                 // [5][16][RP]
+  float* s_red = reinterpret_cast<float*>(qsm + 2 * G::STAGE + G::SV);          // [4][7][16]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(qsm + 2 * G::STAGE + G::SV + G::RED);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   float2 gk[WIN];
   #pragma unroll
@@ -289,68 +424,112 @@ __global__ void __launch_bounds__(kThreads, 3) k_ssim_quad(const SsimQuadJob* __
     asm volatile("" : "+f"(gk[k].x), "+f"(gk[k].y));
   }
   const int wi = WIN == 11 ? 1 : 0;
-  int jb = 0;
-  for(int tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+  if(tid == 0)
   {
-    while(jb + 1 < njobs && jobs[jb + 1].tile_base <= tile) jb++;
+    ptx::mbar_init(&bar[0], 1);
+    ptx::mbar_init(&bar[1], 1);
+    ptx::fence_mbar_init();
+  }
+  __syncthreads();
+
+  // bulk loads of tile `t` (job jn) into stage `sg`: issued by thread 0 only
+  auto issue = [&](int t, int jn, int sg) {
+    const SsimQuadJob& N = jobs[jn];
+    const int local = t - N.tile_base;
+    const int ty = local / N.tiles_x, tx = local - ty * N.tiles_x;
+    const int xr = tx * G::TX, yr = ty * kQTY;
+    // pictures: sample size and resolution of p0 (p1 alike); shift-compensated pictures: uint16
+    const int sb = N.p0.sbytes, sh = N.p0.shift;
+    const uint32_t bytes = 2u * (uint32_t)(quad_box_w(sb, sh) * (sh ? G::BH1 : G::IH) * sb) +
+                           2u * (uint32_t)(quad_box_w(2, 0) * G::IH * 2);
+    fence_proxy_async_shared();
+    ptx::mbar_arrive_expect_tx(&bar[sg], bytes);
+    const unsigned char* tm = reinterpret_cast<const unsigned char*>(N.tmaps);
+    int xs, ys;
+    quad_box_origin(N.p0, xr, yr, xs, ys);
+    ptx::tma_load_2d(qsm + sg * G::STAGE, tm, xs, ys, &bar[sg]);
+    ptx::tma_load_2d(qsm + sg * G::STAGE + G::SLOT, tm + 128, xs, ys, &bar[sg]);
+    quad_box_origin(N.scp1, xr, yr, xs, ys);
+    ptx::tma_load_2d(qsm + sg * G::STAGE + 2 * G::SLOT, tm + 256, xs, ys, &bar[sg]);
+    ptx::tma_load_2d(qsm + sg * G::STAGE + 3 * G::SLOT, tm + 384, xs, ys, &bar[sg]);
+  };
+  auto job_of = [&](int t, int jb) {
+    while(jb + 1 < njobs && jobs[jb + 1].tile_base <= t) jb++;
+    return jb;
+  };
+
+  int jb = 0;
+  uint32_t phase = 0;        // bit s: parity of stage s's next completion
+  uint32_t pend = 0;         // bit s: stage s has bulk loads in flight
+  if(blockIdx.x < ntiles)
+  {
+    jb = job_of(blockIdx.x, 0);
+    if(jobs[jb].tmaps) { if(tid == 0) issue(blockIdx.x, jb, 0); pend |= 1u; }
+  }
+  int it = 0;
+  for(int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, it++)
+  {
+    const int stg = it & 1;
+    jb = job_of(tile, jb);
     const SsimQuadJob& J = jobs[jb];
     const int local = tile - J.tile_base;
     const int ty = local / J.tiles_x, tx = local - ty * J.tiles_x;
     const int x0 = 5 + tx * G::TX, y0 = 5 + ty * kQTY;
     const int x1 = min(x0 + G::TX, J.W - 5), y1 = min(y0 + kQTY, J.H - 5);
-    // staging: all loads first, centring offset = the tile-centre sample of picture 1
-    float v0[G::RPW][2], v1[G::RPW][2], v2[G::RPW][2], v3[G::RPW][2];
-    const float tc = ld_plane(J.p1, min((x0 + x1) >> 1, J.W - 1), min((y0 + y1) >> 1, J.H - 1));
-    load_plane<G::IH>(J.p0, v0, x0 - 5, y0 - 5, J.W, J.H);
-    load_plane<G::IH>(J.p1, v1, x0 - 5, y0 - 5, J.W, J.H);
-    load_plane<G::IH>(J.scp1, v2, x0 - 5, y0 - 5, J.W, J.H);
-    load_plane<G::IH>(J.scp0, v3, x0 - 5, y0 - 5, J.W, J.H);
-    #pragma unroll
-    for(int k = 0; k < G::RPW; k++)
-    {
-      const int i = warp + 8 * k;
-      if(i < G::IH)
-      {
-        s_in[i * kIW + lane] = make_float4(v0[k][0] - tc, v1[k][0] - tc, v2[k][0] - tc, v3[k][0] - tc);
-        s_in[i * kIW + lane + 32] = make_float4(v0[k][1] - tc, v1[k][1] - tc, v2[k][1] - tc, v3[k][1] - tc);
-      }
-    }
-    __syncthreads();
+    const int xr = x0 - 5, yr = y0 - 5;
+    unsigned char* stage = qsm + stg * G::STAGE;
 
-    // vertical pass: column q, output rows 4rg .. 4rg+3; five float2 stream pairs
+    // the next tile's boxes go into the other stage, last read two barriers ago
+    const int nt = tile + gridDim.x;
+    if(nt < ntiles)
+    {
+      const int jn = job_of(nt, jb);
+      if(jobs[jn].tmaps) { if(tid == 0) issue(nt, jn, stg ^ 1); pend |= 1u << (stg ^ 1); }
+    }
+    bool ok = true;
+    if(pend & (1u << stg))
+    {
+      ok = ptx::mbar_wait_bounded(&bar[stg], (phase >> stg) & 1u, kQuadPolls);
+      phase ^= 1u << stg;
+      pend &= ~(1u << stg);
+    }
+    else quad_fill<WIN>(stage, J, xr, yr);
+    if(__syncthreads_or(!ok))
+    { // a bulk load did not arrive: record it, let the other stage's load land, and stop
+      if(tid == 0)
+      {
+        if(J.status) atomicExch(J.status, (int)QMIV_DEVICE_TIMEOUT);
+        if(pend & (1u << (stg ^ 1))) ptx::mbar_wait_bounded(&bar[stg ^ 1], (phase >> (stg ^ 1)) & 1u, kQuadPolls);
+      }
+      __syncthreads();
+      return;
+    }
+
+    // centring offset: the tile-centre sample of picture 1, from its box
+    float tc;
+    {
+      const int xc = min((x0 + x1) >> 1, J.W - 1), yc = min((y0 + y1) >> 1, J.H - 1);
+      int xs, ys;
+      quad_box_origin(J.p1, xr, yr, xs, ys);
+      const int bw = quad_box_w(J.p1.sbytes, J.p1.shift);
+      const int cx = (J.p1.shift ? xc >> 1 : xc) - xs, cy = (J.p1.shift ? yc >> 1 : yc) - ys;
+      const unsigned char* box = stage + G::SLOT;
+      tc = J.p1.sbytes == 1 ? (float)box[cy * bw + cx] : (float)reinterpret_cast<const uint16_t*>(box)[cy * bw + cx];
+    }
+
+    // vertical pass, specialised on the pictures' sample size and resolution
     {
       const int q = tid & (kIW - 1), rg = tid >> 6;
-      const float4* src = s_in + 4 * rg * kIW + q;
-      float2 acc[4][kQPairs];
-      #pragma unroll
-      for(int o = 0; o < 4; o++)
-        #pragma unroll
-        for(int m = 0; m < kQPairs; m++) acc[o][m] = make_float2(0.f, 0.f);
-      #pragma unroll
-      for(int i = 0; i < 3 + WIN; i++)
+      if(J.p0.sbytes == 1)
       {
-        const float4 v = src[i * kIW];          // P0, P1, SCP1, SCP0
-        const float2 sq01 = __fmul2_rn(make_float2(v.x, v.y), make_float2(v.x, v.y));
-        const float2 sq23 = __fmul2_rn(make_float2(v.z, v.w), make_float2(v.z, v.w));
-        float2 st[kQPairs];
-        st[0] = make_float2(v.x, v.y);
-        st[1] = make_float2(v.z, v.w);
-        st[2] = make_float2(sq01.x + sq01.y, v.x * v.y);   // (P0, P1)
-        st[3] = make_float2(sq01.x + sq23.x, v.x * v.z);   // (P0, SCP1)
-        st[4] = make_float2(sq01.y + sq23.y, v.y * v.w);   // (P1, SCP0)
-        #pragma unroll
-        for(int o = 0; o < 4; o++)
-        {
-          const int k = i - o;
-          if(k < 0 || k >= WIN) continue;
-          #pragma unroll
-          for(int m = 0; m < kQPairs; m++) acc[o][m] = __ffma2_rn(gk[k], st[m], acc[o][m]);
-        }
+        if(J.p0.shift) quad_vpass<WIN, uint8_t, 1>(stage, J, xr, yr, tc, gk, s_v, q, rg);
+        else           quad_vpass<WIN, uint8_t, 0>(stage, J, xr, yr, tc, gk, s_v, q, rg);
       }
-      #pragma unroll
-      for(int o = 0; o < 4; o++)
-        #pragma unroll
-        for(int m = 0; m < kQPairs; m++) s_v[(m * kQTY + 4 * rg + o) * kRP + q] = acc[o][m];
+      else
+      {
+        if(J.p0.shift) quad_vpass<WIN, uint16_t, 1>(stage, J, xr, yr, tc, gk, s_v, q, rg);
+        else           quad_vpass<WIN, uint16_t, 0>(stage, J, xr, yr, tc, gk, s_v, q, rg);
+      }
     }
     __syncthreads();
 
@@ -368,7 +547,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_ssim_quad(const SsimQuadJob* __
       {
         float2 val[kQPairs];
         #pragma unroll
-        for(int s2 = 0; s2 < kQPairs; s2++) val[s2] = s_v[(s2 * kQTY + o) * kRP + j0 + t];
+        for(int s2 = 0; s2 < kQPairs; s2++) val[s2] = s_v[(s2 * kQTY + o) * G::RP + j0 + t];
         #pragma unroll
         for(int jj = 0; jj < 4; jj++)
         {
@@ -790,6 +969,9 @@ cudaError_t launch_ssim_quad(const SsimQuadJob* d_jobs, const SsimQuadJob* h_job
     if(e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_quad<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, QGeo<10>::SMEM);
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_quad<11>, cudaFuncAttributeMaxDynamicSharedMemorySize, QGeo<11>::SMEM);
+    // three resident blocks need nearly all of the unified L1 as shared memory
+    if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_quad<10>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_quad<11>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if(e == cudaSuccess)
       e = wi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[1], k_ssim_quad<11>, kThreads, QGeo<11>::SMEM)
              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[0], k_ssim_quad<10>, kThreads, QGeo<10>::SMEM);

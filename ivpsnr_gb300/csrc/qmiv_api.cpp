@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -84,11 +85,12 @@ struct Slot {
   int64_t* stat_rows = nullptr;           // [max_h][6]
   unsigned long long* cps_rows = nullptr; // [2][max_h][3]
   JobScalars* sc = nullptr;
-  // encoded tensor-map sets of the last kTmapSets picture layouts this slot ran (6 x 128 B each,
-  // device), so that a batch repeated over alternating buffers finds its maps without a copy
-  static constexpr int kTmapSets = 16;
+  // encoded tensor-map sets of the last kTmapSets picture layouts this slot ran (up to
+  // kTmapMaps x 128 B each, device: six for the CPS kernel, twelve for the fused SSIM kernel),
+  // so that a batch repeated over alternating buffers finds its maps without a copy
+  static constexpr int kTmapSets = 16, kTmapMaps = 12, kKey = 32;
   uint8_t* d_tmaps = nullptr;
-  uint64_t tmap_key[kTmapSets][16] = { { 0 } };
+  uint64_t tmap_key[kTmapSets][kKey] = { { 0 } };
   uint64_t tmap_stamp[kTmapSets] = { 0 };
   bool tmap_valid[kTmapSets] = { false };
   uint16_t* scp = nullptr;                // 2 pictures x 3 planes x max_w*max_h (IV-SSIM)
@@ -475,22 +477,28 @@ cudaError_t prof_mark(qmiv_handle* h, const char* name, cudaStream_t st, bool be
   return cudaEventRecord(h->prof[h->prof_n++].b, st);
 }
 
-// Encode (or reuse) the six tensor maps a TMA variant reads for one job's planes.
-qmiv_status ensure_tmaps(qmiv_handle* h, DevJob& j, const CpsVariant& v, cudaStream_t st)
+// One 2-D tensor map over a plane of `sb`-byte samples (no swizzle, zeros outside).
+bool encode_plane(CUtensorMap* m, const void* base, int w, int hgt, int stride, int sb, uint32_t bw, uint32_t bh)
 {
-  Slot& S = h->slots[j.slot];
-  const int sb = j.sbytes, XA = 16 / sb, R = v.rows, SR = v.sr, CS = (SR + 1) / 2;
-  const int fd = (R - 1 + SR) / 2;
-  const uint32_t RW = 64 + 2 * XA, TH = R + 2 * SR, CRW = 32 + 2 * XA, CTH = fd + CS + 1;
-  uint64_t key[16] = { 0 };
-  for(int c = 0; c < 3; c++)
-  {
-    key[c] = (uint64_t)(uintptr_t)j.p0[c]; key[3 + c] = (uint64_t)(uintptr_t)j.p1[c];
-    key[6 + c] = ((uint64_t)(uint32_t)j.stride0[c] << 32) | (uint32_t)j.stride1[c];
-  }
-  key[9] = ((uint64_t)(uint32_t)j.W << 32) | (uint32_t)j.H;
-  key[10] = ((uint64_t)RW << 48) | ((uint64_t)TH << 32) | ((uint64_t)CRW << 16) | CTH;
-  key[11] = (uint64_t)sb;
+  EncodeTiledFn enc = encode_fn();
+  if(!enc) return false;
+  const cuuint64_t dims[2] = { (cuuint64_t)w, (cuuint64_t)hgt };
+  const cuuint64_t strides[1] = { (cuuint64_t)stride * sb };
+  const cuuint32_t box[2] = { bw, bh };
+  const cuuint32_t estr[2] = { 1, 1 };
+  return enc(m, sb == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, const_cast<void*>(base), dims,
+             strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// The slot's device copy of the tensor-map set identified by `key` (nmaps maps). A set seen
+// before is reused; a new one is encoded by `encode` into a pinned staging entry and copied
+// over the least recently used set. The copy is stream-ordered after every earlier launch of
+// the handle, so no kernel still reads the set it overwrites.
+template <typename Enc>
+qmiv_status slot_tmaps(qmiv_handle* h, Slot& S, const uint64_t (&key)[Slot::kKey], int nmaps, Enc encode,
+                       cudaStream_t st, const void** out)
+{
   int e = -1, victim = 0;
   for(int t = 0; t < Slot::kTmapSets; t++)
   {
@@ -499,38 +507,106 @@ qmiv_status ensure_tmaps(qmiv_handle* h, DevJob& j, const CpsVariant& v, cudaStr
     if(!S.tmap_valid[t] || S.tmap_stamp[t] < S.tmap_stamp[victim]) victim = t;
   }
   S.tmap_stamp[e >= 0 ? e : victim] = ++h->tmap_clock;
-  if(e >= 0) { j.tmaps = S.d_tmaps + (size_t)e * 6 * sizeof(CUtensorMap); return QMIV_OK; }
-  // a new layout replaces the least recently used set; the copy is stream-ordered after every
-  // earlier launch of the handle, so no kernel still reads the set it overwrites
-  e = victim;
-  j.tmaps = S.d_tmaps + (size_t)e * 6 * sizeof(CUtensorMap);
-  EncodeTiledFn enc = encode_fn();
-  if(!enc) return fail(QMIV_CUDA_ERROR, "cuTensorMapEncodeTiled unavailable");
-  const int nr = (int)h->tmap_ev.size();
-  const int k = h->tmap_next;
-  h->tmap_next = (k + 1) % nr;
-  if(h->tmap_used[k]) CUDA_TRY(cudaEventSynchronize(h->tmap_ev[k]));
-  CUtensorMap* maps = reinterpret_cast<CUtensorMap*>(h->h_tmaps + (size_t)k * 6 * sizeof(CUtensorMap));
-  for(int pic = 0; pic < 2; pic++)
+  if(e < 0)
+  {
+    e = victim;
+    const int nr = (int)h->tmap_ev.size();
+    const int k = h->tmap_next;
+    h->tmap_next = (k + 1) % nr;
+    if(h->tmap_used[k]) CUDA_TRY(cudaEventSynchronize(h->tmap_ev[k]));
+    CUtensorMap* maps = reinterpret_cast<CUtensorMap*>(h->h_tmaps + (size_t)k * Slot::kTmapMaps * sizeof(CUtensorMap));
+    S.tmap_valid[e] = false;
+    if(!encode(maps)) return fail(QMIV_CUDA_ERROR, "cuTensorMapEncodeTiled failed");
+    CUDA_TRY(cudaMemcpyAsync(S.d_tmaps + (size_t)e * Slot::kTmapMaps * sizeof(CUtensorMap), maps,
+                             (size_t)nmaps * sizeof(CUtensorMap), cudaMemcpyHostToDevice, st));
+    CUDA_TRY(cudaEventRecord(h->tmap_ev[k], st));
+    h->tmap_used[k] = 1;
+    std::memcpy(S.tmap_key[e], key, sizeof(key));
+    S.tmap_valid[e] = true;
+  }
+  *out = S.d_tmaps + (size_t)e * Slot::kTmapMaps * sizeof(CUtensorMap);
+  return QMIV_OK;
+}
+
+// Encode (or reuse) the six tensor maps a TMA variant reads for one job's planes.
+qmiv_status ensure_tmaps(qmiv_handle* h, DevJob& j, const CpsVariant& v, cudaStream_t st)
+{
+  Slot& S = h->slots[j.slot];
+  const int sb = j.sbytes, XA = 16 / sb, R = v.rows, SR = v.sr, CS = (SR + 1) / 2;
+  const int fd = (R - 1 + SR) / 2;
+  const uint32_t RW = 64 + 2 * XA, TH = R + 2 * SR, CRW = 32 + 2 * XA, CTH = fd + CS + 1;
+  uint64_t key[Slot::kKey] = { 0 };
+  key[0] = 1;  // CPS set
+  for(int c = 0; c < 3; c++)
+  {
+    key[1 + c] = (uint64_t)(uintptr_t)j.p0[c]; key[4 + c] = (uint64_t)(uintptr_t)j.p1[c];
+    key[7 + c] = ((uint64_t)(uint32_t)j.stride0[c] << 32) | (uint32_t)j.stride1[c];
+  }
+  key[10] = ((uint64_t)(uint32_t)j.W << 32) | (uint32_t)j.H;
+  key[11] = ((uint64_t)RW << 48) | ((uint64_t)TH << 32) | ((uint64_t)CRW << 16) | CTH;
+  key[12] = (uint64_t)sb;
+  auto encode = [&](CUtensorMap* maps) {
+    for(int pic = 0; pic < 2; pic++)
+      for(int c = 0; c < 3; c++)
+      {
+        const void* base = pic == 0 ? j.p0[c] : j.p1[c];
+        const int stride = pic == 0 ? j.stride0[c] : j.stride1[c];
+        if(!encode_plane(&maps[pic * 3 + c], base, c ? j.W / 2 : j.W, c ? j.H / 2 : j.H, stride, sb, c ? CRW : RW, c ? CTH : TH))
+          return false;
+      }
+    return true;
+  };
+  return slot_tmaps(h, S, key, 6, encode, st, &j.tmaps);
+}
+
+// Can a tensor map describe this plane? 16-byte aligned base and pitch, 8/16-bit samples.
+bool plane_tma_ok(const SsimPlane& p)
+{
+  return p.ptr && (p.sbytes == 1 || p.sbytes == 2) && ((uintptr_t)p.ptr & 15) == 0 && ((size_t)p.stride * p.sbytes) % 16 == 0;
+}
+
+// Tensor maps of a frame's three fused-SSIM jobs (four planes each), or null maps for a frame
+// whose planes a tensor map cannot describe (the kernel then stages them with plain loads).
+qmiv_status ensure_quad_tmaps(qmiv_handle* h, Slot& S, SsimQuadJob* q, cudaStream_t st)
+{
+  bool ok = encode_fn() != nullptr;
+  for(int c = 0; c < 3 && ok; c++)
+    ok = plane_tma_ok(q[c].p0) && plane_tma_ok(q[c].p1) && plane_tma_ok(q[c].scp1) && plane_tma_ok(q[c].scp0) &&
+         q[c].scp1.sbytes == 2 && q[c].scp1.shift == 0 && q[c].scp0.sbytes == 2 && q[c].scp0.shift == 0;
+  if(!ok) { for(int c = 0; c < 3; c++) q[c].tmaps = nullptr; return QMIV_OK; }
+  const int win = h->opt.ssim_window;
+  uint64_t key[Slot::kKey] = { 0 };
+  key[0] = 2;  // fused-SSIM set
+  key[1] = ((uint64_t)(uint32_t)q[0].W << 32) | (uint32_t)q[0].H;
+  key[2] = ((uint64_t)(uint32_t)win << 32) | ((uint32_t)q[0].p0.sbytes << 8);
+  for(int c = 0; c < 3; c++)
+  {
+    const SsimPlane* pl[4] = { &q[c].p0, &q[c].p1, &q[c].scp1, &q[c].scp0 };
+    for(int k = 0; k < 4; k++)
+    {
+      key[3 + c * 8 + 2 * k] = (uint64_t)(uintptr_t)pl[k]->ptr;
+      key[4 + c * 8 + 2 * k] = ((uint64_t)(uint32_t)pl[k]->stride << 8) | (uint64_t)(uint8_t)pl[k]->shift;
+    }
+  }
+  auto encode = [&](CUtensorMap* maps) {
     for(int c = 0; c < 3; c++)
     {
-      const void* base = pic == 0 ? j.p0[c] : j.p1[c];
-      const int stride = pic == 0 ? j.stride0[c] : j.stride1[c];
-      const cuuint64_t dims[2] = { (cuuint64_t)(c ? j.W / 2 : j.W), (cuuint64_t)(c ? j.H / 2 : j.H) };
-      const cuuint64_t strides[1] = { (cuuint64_t)stride * sb };
-      const cuuint32_t box[2] = { c ? CRW : RW, c ? CTH : TH };
-      const cuuint32_t estr[2] = { 1, 1 };
-      CUresult r = enc(&maps[pic * 3 + c], sb == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_UINT16, 2,
-                       const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                       CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-      if(r != CUDA_SUCCESS) { S.tmap_valid[e] = false; return fail(QMIV_CUDA_ERROR, "cuTensorMapEncodeTiled failed (%d)", (int)r); }
+      const SsimPlane* pl[4] = { &q[c].p0, &q[c].p1, &q[c].scp1, &q[c].scp0 };
+      for(int k = 0; k < 4; k++)
+      {
+        const SsimPlane& P = *pl[k];
+        const int wp = P.shift ? q[c].W / 2 : q[c].W, hp = P.shift ? q[c].H / 2 : q[c].H;
+        if(!encode_plane(&maps[c * 4 + k], P.ptr, wp, hp, P.stride, P.sbytes, (uint32_t)quad_box_w(P.sbytes, P.shift),
+                         (uint32_t)quad_box_h(win, P.shift)))
+          return false;
+      }
     }
-  CUDA_TRY(cudaMemcpyAsync(S.d_tmaps + (size_t)e * 6 * sizeof(CUtensorMap), maps, 6 * sizeof(CUtensorMap),
-                           cudaMemcpyHostToDevice, st));
-  CUDA_TRY(cudaEventRecord(h->tmap_ev[k], st));
-  h->tmap_used[k] = 1;
-  std::memcpy(S.tmap_key[e], key, sizeof(key));
-  S.tmap_valid[e] = true;
+    return true;
+  };
+  const void* d = nullptr;
+  qmiv_status s = slot_tmaps(h, S, key, 12, encode, st, &d);
+  if(s != QMIV_OK) return s;
+  for(int c = 0; c < 3; c++) q[c].tmaps = static_cast<const uint8_t*>(d) + (size_t)c * 4 * sizeof(CUtensorMap);
   return QMIV_OK;
 }
 
@@ -562,7 +638,7 @@ void add_ssim_job(qmiv_handle* h, const SsimPlane& a, const SsimPlane& b, int W,
 }
 
 // SSIM jobs, pyramid steps and the combine entry of one frame (a job with SSIM metrics).
-qmiv_status plan_ssim(qmiv_handle* h, const DevJob& j)
+qmiv_status plan_ssim(qmiv_handle* h, const DevJob& j, cudaStream_t st)
 {
   Slot& S = h->slots[j.slot];
   const int W = j.W, H = j.H, bd = j.bd, sb = j.sbytes, cs = j.cshift;
@@ -595,8 +671,11 @@ qmiv_status plan_ssim(qmiv_handle* h, const DevJob& j)
         add_ssim_job(h, P0[c], P1[c], W, H, bd, 1, part, outs[k]);
         h->sjobs.back().tiles_y = 0;  // finalisation only
       }
+      q.status = reinterpret_cast<int32_t*>(reinterpret_cast<char*>(j.result) + offsetof(qmiv_frame_result, status));
       h->qjobs.push_back(q);
     }
+    qmiv_status ts = ensure_quad_tmaps(h, S, &h->qjobs[h->qjobs.size() - 3], st);
+    if(ts != QMIV_OK) return ts;
   }
   else if(j.metrics & QMIV_M_SSIM)   // xAppQMIV.cpp:907: calcPicSSIM(P0, P1)
     for(int c = 0; c < 3; c++) add_ssim_job(h, P0[c], P1[c], W, H, bd, 1, part, S.vals + c);
@@ -723,7 +802,7 @@ qmiv_status plan_jobs(qmiv_handle* h, LaunchPlan& P, cudaStream_t st)
   h->sjobs.clear(); h->frames.clear(); h->qjobs.clear();
   for(int s = 0; s < 4; s++) h->steps[s].clear();
   for(int i = 0; i < n; i++)
-    if(h->jobs[i].metrics & kSsimMetrics) { qmiv_status ps = plan_ssim(h, h->jobs[i]); if(ps != QMIV_OK) return ps; }
+    if(h->jobs[i].metrics & kSsimMetrics) { qmiv_status ps = plan_ssim(h, h->jobs[i], st); if(ps != QMIV_OK) return ps; }
   int tb = 0;
   for(auto& s : h->sjobs) { s.tile_base = tb; tb += s.tiles_x * s.tiles_y; }
   tb = 0;
@@ -914,7 +993,7 @@ qmiv_status qmiv_create(qmiv_handle** out, const qmiv_options* opt, int32_t max_
   const size_t rows_b = align256((size_t)max_h * 6 * sizeof(int64_t));
   const size_t cps_b = align256((size_t)2 * max_h * 3 * sizeof(unsigned long long));
   const size_t sc_b = align256(sizeof(JobScalars));
-  const size_t tm_b = align256((size_t)Slot::kTmapSets * 6 * 128);
+  const size_t tm_b = align256((size_t)Slot::kTmapSets * Slot::kTmapMaps * 128);
   const size_t per = rows_b + cps_b + sc_b + tm_b;
   if(cudaMalloc(&h->slot_mem, per * max_jobs) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "slot scratch %zu B", per * max_jobs));
   if(cudaMemset(h->slot_mem, 0, per * max_jobs) != cudaSuccess) return cleanup(fail(QMIV_CUDA_ERROR, "memset"));
@@ -981,7 +1060,7 @@ qmiv_status qmiv_create(qmiv_handle** out, const qmiv_options* opt, int32_t max_
   }
   {
     const int nr = 2 * max_jobs + 4;
-    if(cudaMallocHost(&h->h_tmaps, (size_t)nr * 6 * sizeof(CUtensorMap)) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "pinned tensor maps"));
+    if(cudaMallocHost(&h->h_tmaps, (size_t)nr * Slot::kTmapMaps * sizeof(CUtensorMap)) != cudaSuccess) return cleanup(fail(QMIV_OUT_OF_MEMORY, "pinned tensor maps"));
     h->tmap_ev.assign(nr, nullptr);
     h->tmap_used.assign(nr, 0);
     for(int k = 0; k < nr; k++)
@@ -1461,7 +1540,7 @@ struct qmiv_graph {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   uint8_t* d_tab = nullptr;     // the batch's own tables
-  uint8_t* d_tmaps = nullptr;   // the batch's own tensor maps (6 per job)
+  uint8_t* d_tmaps = nullptr;   // the batch's own tensor maps (6 per job, 4 per fused-SSIM job)
   int64_t launches = 0;         // kernels per replay
 };
 
@@ -1495,7 +1574,8 @@ qmiv_status qmiv_batch_graph_create(qmiv_handle* h, const qmiv_job* jobs, int32_
   g->h = h;
   auto bail = [&](qmiv_status e) { qmiv_batch_graph_destroy(g); return e; };
   // private copies of the tensor maps and tables: later calls on the handle rewrite the slots'
-  if(cudaMalloc(&g->d_tmaps, (size_t)n * 6 * sizeof(CUtensorMap)) != cudaSuccess) return bail(fail(QMIV_OUT_OF_MEMORY, "graph tensor maps"));
+  const size_t nq = h->qjobs.size();
+  if(cudaMalloc(&g->d_tmaps, ((size_t)n * 6 + nq * 4) * sizeof(CUtensorMap)) != cudaSuccess) return bail(fail(QMIV_OUT_OF_MEMORY, "graph tensor maps"));
   for(int i = 0; i < n; i++)
   {
     DevJob& j = h->jobs[i];
@@ -1504,6 +1584,15 @@ qmiv_status qmiv_batch_graph_create(qmiv_handle* h, const qmiv_job* jobs, int32_
     if(cudaMemcpyAsync(dst, j.tmaps, 6 * sizeof(CUtensorMap), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
       return bail(fail(QMIV_CUDA_ERROR, "graph tensor maps copy"));
     j.tmaps = dst;
+  }
+  for(size_t i = 0; i < nq; i++)
+  {
+    SsimQuadJob& q = h->qjobs[i];
+    if(!q.tmaps) continue;
+    uint8_t* dst = g->d_tmaps + ((size_t)n * 6 + i * 4) * sizeof(CUtensorMap);
+    if(cudaMemcpyAsync(dst, q.tmaps, 4 * sizeof(CUtensorMap), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+      return bail(fail(QMIV_CUDA_ERROR, "graph tensor maps copy"));
+    q.tmaps = dst;
   }
   std::vector<uint8_t> img(h->tab.bytes);
   const size_t bytes = pack_tables(h, img.data(), img.size());

@@ -40,8 +40,14 @@ struct SsimQuadJob {
   int32_t tiles_x, tiles_y, tile_base;
   uint32_t outs;
   float* partial[4];
+  const void* tmaps;     // 4 tensor maps (p0, p1, scp1, scp0 boxes) or null: staged by plain loads
+  int32_t* status;       // the frame's result status (a bulk load that never arrived), or null
 };
 int ssim_quad_tiles_y(int H);
+// Box of one plane of a fused-kernel tile: width (samples) for `sb`-byte samples at full (shift 0)
+// or half resolution, and height for the window (QMIV_SSIM_*).
+__host__ __device__ constexpr int quad_box_w(int sb, int shift) { return (shift ? 32 : 64) + 16 / sb; }
+int quad_box_h(int window, int shift);
 cudaError_t launch_ssim_quad(const SsimQuadJob* d_jobs, const SsimQuadJob* h_jobs, int n, int window, cudaStream_t st);
 
 // One DownsampleHV step of the MS-SSIM pyramid.

@@ -164,3 +164,36 @@ def test_ssim_family_matches_reference_golden(gpu_lib, case):
     np.testing.assert_allclose(g["msssim"][:3], e["msssim"], atol=TOL)
     for k in ("ivssim", "ivssim_r2t", "ivssim_t2r"):
         assert abs(g[k] - e[k]) <= TOL
+
+
+@pytest.mark.parametrize("w,h,bd,cf444,window", [(320, 180, 10, False, 0), (256, 144, 8, False, 0),
+                                                 (192, 128, 10, True, 0), (200, 120, 10, False, 1)])
+def test_fused_staging_paths_agree(gpu_lib, oq, w, h, bd, cf444, window):
+    """The fused SSIM kernel stages 16-byte aligned planes with bulk-tensor loads and other planes
+    with plain loads; both must give identical values (they differ only in samples that feed no
+    valid output). The unaligned copies sit 3 samples into rows 3 samples wider."""
+    import torch
+    from oracle.oracle import upsample420
+    ref, tst = synth.pair420(w, h, bd, seed=300 + w, holes=True)
+    dtype = np.uint8 if bd == 8 else np.uint16
+    if cf444:
+        p0 = [np.ascontiguousarray(p.astype(dtype)) for p in upsample420(synth.split420(ref, w, h), w, h)]
+        p1 = [np.ascontiguousarray(p.astype(dtype)) for p in upsample420(synth.split420(tst, w, h), w, h)]
+    else:
+        p0, p1 = _planes(ref, w, h, dtype), _planes(tst, w, h, dtype)
+    tview = lambda a: torch.from_numpy(a.view(np.int16) if a.dtype == np.uint16 else a)
+    aligned = [[tview(p).cuda() for p in ps] for ps in (p0, p1)]
+    def padded(p):
+        buf = torch.zeros((p.shape[0], p.shape[1] + 3), dtype=tview(p).dtype, device="cuda")
+        buf[:, 3:] = tview(p).cuda()
+        return buf[:, 3:]
+    unaligned = [[padded(p) for p in ps] for ps in (p0, p1)]
+    cf = gpu_lib.CF444 if cf444 else gpu_lib.CF420
+    with gpu_lib.Processor(w, h, ssim_window=window) as P:
+        a = P.calc_frame(gpu_lib.make_pic(aligned[0], bd, cf), gpu_lib.make_pic(aligned[1], bd, cf), gpu_lib.M_ALL)
+        b = P.calc_frame(gpu_lib.make_pic(unaligned[0], bd, cf), gpu_lib.make_pic(unaligned[1], bd, cf), gpu_lib.M_ALL)
+    for k in ("ssim", "msssim", "ssim_pic", "msssim_pic", "ivssim", "ivssim_r2t", "ivssim_t2r", "ivpsnr", "psnr"):
+        assert a[k] == b[k], (k, a[k], b[k])
+    o = oq.frame(upsample420(synth.split420(ref, w, h), w, h), upsample420(synth.split420(tst, w, h), w, h), bd, True,
+                 ssim_window=window, nthreads=8)
+    _cmp_ssim(a, o)
