@@ -110,6 +110,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_ssim(const SsimJob* __restrict_
 {
   using G = SGeo<WIN>;
   extern __shared__ __align__(16) float smem[];
+  __shared__ float s_kcc;  // (1 - W0) tc^2 W0 of the current tile, formed in FP64 by one thread
   float2* s_in = reinterpret_cast<float2*>(smem);                    // [IH][64]
   float4* s_v = reinterpret_cast<float4*>(smem + 2 * G::IH * kIW);   // [32][kRP]
   float* s_red = smem + 2 * G::IH * kIW + 4 * kTY * kRP;             // [7][32]
@@ -139,6 +140,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_ssim(const SsimJob* __restrict_
     const float tc = ld_plane(J.b, min((x0 + x1) >> 1, J.W - 1), min((y0 + y1) >> 1, J.H - 1));
     load_plane<G::IH>(J.a, va, x0 - 5, y0 - 5, J.W, J.H);
     load_plane<G::IH>(J.b, vb, x0 - 5, y0 - 5, J.W, J.H);
+    if(tid == 0) s_kcc = (float)(c_omd[wi] * (double)tc * (double)tc * c_w0d[wi]);  // one FP64 product per tile
     #pragma unroll
     for(int k = 0; k < G::RPW; k++)
     {
@@ -201,7 +203,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_ssim(const SsimJob* __restrict_
         }
       }
       const float cf = tc;
-      const float k_cc = (float)(c_omd[wi] * (double)tc * (double)tc * c_w0d[wi]);
+      const float k_cc = s_kcc;
       const float cw0 = cf * c_w0[wi], om2c = c_om[wi] * 2.0f * cf, omc = c_om[wi] * cf;
       const float vq0 = 2.0f * k_cc + J.c2, cv0 = k_cc, C1 = J.c1, C2 = J.c2;
       const bool calc_l = J.calc_l != 0;
@@ -412,6 +414,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_ssim_quad(const SsimQuadJob* __
 {
   using G = QGeo<WIN>;
   extern __shared__ __align__(128) unsigned char qsm[];
+  __shared__ float s_kcc;  // (1 - W0) tc^2 W0 of the current tile, formed in FP64 by one thread
   float2* s_v = reinterpret_cast<float2*>(qsm + 2 * G::STAGE);                 // [5][16][RP]
   float* s_red = reinterpret_cast<float*>(qsm + 2 * G::STAGE + G::SV);          // [4][7][16]
   uint64_t* bar = reinterpret_cast<uint64_t*>(qsm + 2 * G::STAGE + G::SV + G::RED);
@@ -515,6 +518,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_ssim_quad(const SsimQuadJob* __
       const int cx = (J.p1.shift ? xc >> 1 : xc) - xs, cy = (J.p1.shift ? yc >> 1 : yc) - ys;
       const unsigned char* box = stage + G::SLOT;
       tc = J.p1.sbytes == 1 ? (float)box[cy * bw + cx] : (float)reinterpret_cast<const uint16_t*>(box)[cy * bw + cx];
+      if(tid == 0) s_kcc = (float)(c_omd[wi] * (double)tc * (double)tc * c_w0d[wi]);
     }
 
     // vertical pass, specialised on the pictures' sample size and resolution
@@ -558,7 +562,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_ssim_quad(const SsimQuadJob* __
         }
       }
       const float cf = tc;
-      const float k_cc = (float)(c_omd[wi] * (double)tc * (double)tc * c_w0d[wi]);
+      const float k_cc = s_kcc;
       const float cw0 = cf * c_w0[wi], om2c = c_om[wi] * 2.0f * cf, omc = c_om[wi] * cf;
       const float C1 = J.c1, C2 = J.c2;
       const bool row_ok = y0 + o < y1;
@@ -730,6 +734,8 @@ __global__ void __launch_bounds__(256, 3) k_ssim_bwd(const SsimBwdJob* __restric
   const int px0 = qx0 - (WIN - 6), py0 = qy0 - (WIN - 6);  // p = q - k, k in [-5, WIN-6]
   const int sx0 = px0 - 5, sy0 = py0 - 5;
   const float c = __ldg((const float*)J.b.ptr + (int64_t)min(qy0 + kBwdT / 2, H - 1) * J.b.stride + min(qx0 + kBwdT / 2, W - 1));
+  __shared__ float s_kcc;  // (1 - W0) c^2 W0, formed in FP64 by one thread (read after the next barrier)
+  if(tid == 0) s_kcc = (float)(c_omd[WIN == 11 ? 1 : 0] * (double)c * (double)c * c_w0d[WIN == 11 ? 1 : 0]);
   const float* pa = (const float*)J.a.ptr;
   const float* pb = (const float*)J.b.ptr;
   { // all loads of the tile are issued before the first store
@@ -780,7 +786,7 @@ __global__ void __launch_bounds__(256, 3) k_ssim_bwd(const SsimBwdJob* __restric
   // thread = p row x 8 consecutive p columns
   const int wi = WIN == 11 ? 1 : 0;
   const float w0 = c_w0[wi], om = c_om[wi];
-  const float k_cc = (float)(c_omd[wi] * (double)c * (double)c * c_w0d[wi]);
+  const float k_cc = s_kcc;
   const float C1 = J.c1, C2 = J.c2;
   for(int it = tid; it < PW * NG; it += 256)
   {
