@@ -34,6 +34,14 @@ struct Geo {
 };
 
 // ---- global colour difference ---------------------------------------------------------------
+// Knuth's TwoSum: a + b = s + e exactly in round-to-nearest FP32.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e)
+{
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
 __global__ void __launch_bounds__(256) k_loss_gcd_part(Geo g, double* __restrict__ part)
 {
   __shared__ double scratch[16];
@@ -42,9 +50,19 @@ __global__ void __launch_bounds__(256) k_loss_gcd_part(Geo g, double* __restrict
   const int64_t b0 = (int64_t)blockIdx.x * per, b1 = min(g.plane, b0 + per);
   const float* r = g.ref + (int64_t)pc * g.plane;
   const float* t = g.tst + (int64_t)pc * g.plane;
-  double acc = 0.0;  // FP32 differences are exact in FP64; a thread adds a few hundred of them
-  for(int64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) acc += (double)__ldg(r + i) - (double)__ldg(t + i);
-  Kbns k = { acc, 0.0 };
+  // Each difference r - t is taken exactly as an unevaluated FP32 pair (TwoSum) and added to a
+  // running (hi, lo) pair: hi by TwoSum, lo collects the exact errors. FP32 only, since FP64
+  // arithmetic per element runs far below the memory rate here; the thread's pair goes to FP64
+  // once, for the block's compensated sum.
+  float hi = 0.0f, lo = 0.0f;
+  for(int64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x)
+  {
+    float d, de, e;
+    two_sum(__ldg(r + i), -__ldg(t + i), d, de);
+    two_sum(hi, d, hi, e);
+    lo = __fadd_rn(lo, __fadd_rn(e, de));
+  }
+  Kbns k = { (double)hi, (double)lo };
   const double s = block_kbns(k, scratch);
   if(threadIdx.x == 0) part[pc * kLossGcdChunks + blockIdx.x] = s;
 }
@@ -137,7 +155,10 @@ __global__ void __launch_bounds__(kCpsTX * kCpsTY) k_loss_cps(Geo g, float w0, f
       }
     const int c1x = min(max(x + k1 % (2 * SR + 1) - SR, 0), g.W - 1) - x0 + SR, c1y = min(max(y + k1 / (2 * SR + 1) - SR, 0), g.H - 1) - y0 + SR;
     const int c0x = min(max(x + k0 % (2 * SR + 1) - SR, 0), g.W - 1) - x0 + SR, c0y = min(max(y + k0 / (2 * SR + 1) - SR, 0), g.H - 1) - y0 + SR;
-    int m1 = k1, m0 = k0;
+    // stored index: the clamped displacement's position in the window, so that a pixel's
+    // target is p + (k % side - SR, k / side - SR) without clamping and the gradient gather can
+    // test "does p map to q" with one comparison
+    int m1 = (c1y - ly) * (2 * SR + 1) + (c1x - lx), m0 = (c0y - ly) * (2 * SR + 1) + (c0x - lx);
     const int64_t pix = (int64_t)y * g.W + x;
     float* scp1 = scp + (int64_t)b * 3 * g.plane;
     float* scp0 = scp + ((int64_t)g.n + b) * 3 * g.plane;
@@ -301,14 +322,16 @@ __global__ void __launch_bounds__(256) k_loss_grad(BwdArgs a)
     const float e1 = __fsub_rn(__fadd_rn(tq[c], s_f[3][c]), R[(int64_t)c * g.plane + q1]);
     acc[c] = a.g_tst[((int64_t)b * 3 + c) * g.plane + q] + s_f[0][c] * e1 + s_f[2][c];
   }
-  // pixels p whose T2R argmin reads q lie within the window around q
+  // pixels p = q + (dx, dy) whose T2R argmin reads q: those whose stored (clamped) displacement
+  // is (-dx, -dy); the halo's 0xffff never matches
+  #pragma unroll
   for(int dy = -sr; dy <= sr; dy++)
+    #pragma unroll
     for(int dx = -sr; dx <= sr; dx++)
     {
       const int m0 = s_m0[ly + kLossMaxSR + dy][lx + kLossMaxSR + dx];
-      if(m0 == 0xffff) continue;
-      const int k0 = m0 & 255, px = x + dx, py = y + dy;
-      if(clampi(px + k0 % side - sr, 0, g.W - 1) != x || clampi(py + k0 / side - sr, 0, g.H - 1) != y) continue;
+      if((m0 & 255) != (sr - dy) * side + (sr - dx)) continue;
+      const int px = x + dx, py = y + dy;
       const int64_t p = (int64_t)py * g.W + px;
       #pragma unroll
       for(int c = 0; c < 3; c++)

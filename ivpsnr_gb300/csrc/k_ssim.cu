@@ -950,6 +950,9 @@ cudaError_t launch_ssim_bwd(const SsimBwdJob* d_jobs, const SsimBwdJob* h_jobs, 
   {
     cudaError_t e = cudaFuncSetAttribute(k_ssim_bwd<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, BGeo<10>::SMEM);
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_bwd<11>, cudaFuncAttributeMaxDynamicSharedMemorySize, BGeo<11>::SMEM);
+    // three resident blocks of 68-72 KB need the unified L1 mostly as shared memory
+    if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_bwd<10>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_bwd<11>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if(e != cudaSuccess) return e;
     attr = true;
   }
