@@ -15,9 +15,11 @@
 // [lo, hi] inclusive, and GCD contributes -1/Area per pixel while it is not clipped.
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "qmiv_device.cuh"
+
 #include "qmiv_loss.h"
 
 namespace qmiv {
@@ -128,8 +130,10 @@ __global__ void __launch_bounds__(kCpsTX * kCpsTY) k_loss_cps(Geo g, float w0, f
   const int x = x0 + lx, y = y0 + ly;
   const bool inside = x < g.W && y < g.H;
   float e1[3] = { 0.f, 0.f, 0.f }, e0[3] = { 0.f, 0.f, 0.f };
-  if(inside)
-  {
+  // tiles whose windows stay inside the picture read their candidates without clamping
+  const bool interior = x0 >= SR && y0 >= SR && x0 + kCpsTX + SR <= g.W && y0 + kCpsTY + SR <= g.H;
+  auto search = [&](auto in_tag) {
+  constexpr bool IN = decltype(in_tag)::value;
     float gc[3], tg[3], rg[3];
     for(int c = 0; c < 3; c++)
     {
@@ -145,8 +149,8 @@ __global__ void __launch_bounds__(kCpsTX * kCpsTY) k_loss_cps(Geo g, float w0, f
       for(int dx = 0; dx <= 2 * SR; dx++)
       {
         // clamped candidate (x+dx-SR, y+dy-SR) in staged coordinates
-        const int cx = min(max(x + dx - SR, 0), g.W - 1) - x0 + SR;
-        const int cy = min(max(y + dy - SR, 0), g.H - 1) - y0 + SR;
+        const int cx = IN ? lx + dx : min(max(x + dx - SR, 0), g.W - 1) - x0 + SR;
+        const int cy = IN ? ly + dy : min(max(y + dy - SR, 0), g.H - 1) - y0 + SR;
         const float E1 = werr(__fsub_rn(tg[0], s_r[0][cy][cx]), __fsub_rn(tg[1], s_r[1][cy][cx]), __fsub_rn(tg[2], s_r[2][cy][cx]), w0, w1, w2);
         const float E0 = werr(__fsub_rn(rg[0], s_t[0][cy][cx]), __fsub_rn(rg[1], s_t[1][cy][cx]), __fsub_rn(rg[2], s_t[2][cy][cx]), w0, w1, w2);
         const int k = dy * (2 * SR + 1) + dx;
@@ -175,6 +179,11 @@ __global__ void __launch_bounds__(kCpsTX * kCpsTY) k_loss_cps(Geo g, float w0, f
     }
     maps[(int64_t)b * g.plane + pix] = (uint16_t)m1;
     maps[((int64_t)g.n + b) * g.plane + pix] = (uint16_t)m0;
+  };
+  if(inside)
+  {
+    if(interior) search(std::true_type{});
+    else         search(std::false_type{});
   }
   // per-block SSE partials: [R2T c0..2, T2R c0..2]
   float v[6] = { e1[0] * e1[0], e1[1] * e1[1], e1[2] * e1[2], e0[0] * e0[0], e0[1] * e0[1], e0[2] * e0[2] };
