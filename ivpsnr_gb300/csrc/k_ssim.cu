@@ -690,12 +690,12 @@ template <int WIN> struct BGeo {
   // row pitches (float4) read down a column by consecutive lanes are odd: conflict-free
   static constexpr int VP = SW | 1, MP = PW | 1;
   // region A: staged samples [SW][SW] float2, later the coefficient maps [PW][MP] float4;
-  // region B: vertical sums [PW][VP] float4, later F [32][MP] float4; the tile's own centred
+  // region B: vertical sums [PW][VP] float4, later F [PW][33] float4; the tile's own centred
   // samples [32][32] float2
   static constexpr int A = (SW * SW * 8 > PW * MP * 16 ? SW * SW * 8 : PW * MP * 16);
   static constexpr int B = PW * VP * 16;
   static constexpr int SMEM = A + B + kBwdT * kBwdT * 8;
-  static_assert(kBwdT * MP <= PW * VP, "F aliases V");
+  static_assert(PW * (kBwdT + 1) <= PW * VP && kBwdT * kBwdT / 4 == 256, "F aliases V; one q column x 4 rows per thread");
 };
 
 // acc += g * v on a float4 as two packed FP32 multiply-adds
@@ -717,7 +717,7 @@ __global__ void __launch_bounds__(256, 3) k_ssim_bwd(const SsimBwdJob* __restric
   float2* s_in = reinterpret_cast<float2*>(smem);                    // A: [SW][SW] centred a, b
   float4* s_m = reinterpret_cast<float4*>(smem);                     // A: [PW][MP] coefficient maps
   float4* s_v = reinterpret_cast<float4*>(smem + G::A / 4);          // B: [PW][VP] vertical sums
-  float4* s_f = s_v;                                                 // B: [32][MP]
+  float4* s_f = s_v;                                                 // B: [PW][33]
   float2* s_q = reinterpret_cast<float2*>(smem + (G::A + G::B) / 4); // [32][32] centred a, b at q
   float2 gk[WIN];
   #pragma unroll
@@ -830,53 +830,56 @@ __global__ void __launch_bounds__(256, 3) k_ssim_bwd(const SsimBwdJob* __restric
     }
   }
   __syncthreads();
-  // transposed vertical pass: F[qr][pc] = sum_j g[j] M[qr + WIN-1-j][pc];
-  // thread = p column x 8 consecutive q rows (F reuses the V area)
+  // transposed horizontal pass: F[pr][qc] = sum_j g[j] M[pr][qc + WIN-1-j];
+  // thread = p row x 8 consecutive q columns (F reuses the V area, pitch FP float4)
+  constexpr int FP = kBwdT + 1;
   for(int it = tid; it < PW * (kBwdT / 8); it += 256)
   {
-    const int pc = it % PW, q0 = 8 * (it / PW);
+    const int r = it % PW, q0 = 8 * (it / PW);
     float4 acc[8];
     #pragma unroll
     for(int o = 0; o < 8; o++) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
     #pragma unroll
     for(int i = 0; i < 7 + WIN; i++)
     {
-      const float4 v = s_m[(q0 + i) * MP + pc];
+      const float4 v = s_m[r * MP + q0 + i];
       #pragma unroll
       for(int o = 0; o < 8; o++)
         if(o + WIN - 1 - i >= 0 && o + WIN - 1 - i < WIN) fma4(gk[o + WIN - 1 - i], v, acc[o]);
     }
     #pragma unroll
-    for(int o = 0; o < 8; o++) s_f[(q0 + o) * MP + pc] = acc[o];
+    for(int o = 0; o < 8; o++) s_f[r * FP + q0 + o] = acc[o];
   }
   __syncthreads();
-  // transposed horizontal pass and the combination: thread = q row x 8 consecutive q columns
+  // transposed vertical pass and the combination: thread = q column x 4 consecutive q rows, so
+  // that all 256 threads work and a warp's stores cover consecutive columns of a row
   const float scale = (float)(*J.g / ((double)W * (double)H));
-  for(int it = tid; it < kBwdT * (kBwdT / 8); it += 256)
   {
-    const int r = it % kBwdT, q0 = 8 * (it / kBwdT);
-    const int y = qy0 + r;
-    float4 acc[8];
+    const int cq = tid % kBwdT, q0 = 4 * (tid / kBwdT);
+    const int x = qx0 + cq;
+    float4 acc[4];
     #pragma unroll
-    for(int o = 0; o < 8; o++) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for(int o = 0; o < 4; o++) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
     #pragma unroll
-    for(int i = 0; i < 7 + WIN; i++)
+    for(int i = 0; i < 3 + WIN; i++)
     {
-      const float4 v = s_f[r * MP + q0 + i];
+      const float4 v = s_f[(q0 + i) * FP + cq];
       #pragma unroll
-      for(int o = 0; o < 8; o++)
+      for(int o = 0; o < 4; o++)
         if(o + WIN - 1 - i >= 0 && o + WIN - 1 - i < WIN) fma4(gk[o + WIN - 1 - i], v, acc[o]);
     }
-    if(y >= H) continue;
-    #pragma unroll
-    for(int o = 0; o < 8; o++)
+    if(x < W)
     {
-      const int x = qx0 + q0 + o;
-      if(x >= W) break;
-      const float4 f = acc[o];
-      const float2 v = s_q[r * kBwdT + q0 + o];  // the centred samples at q
-      if(J.outx) J.outx[(int64_t)y * W + x] = scale * (f.x + 2.0f * v.x * f.z + v.y * f.w);
-      if(J.outy) J.outy[(int64_t)y * W + x] = scale * (f.y + 2.0f * v.y * f.z + v.x * f.w);
+      #pragma unroll
+      for(int o = 0; o < 4; o++)
+      {
+        const int y = qy0 + q0 + o;
+        if(y >= H) break;
+        const float4 f = acc[o];
+        const float2 v = s_q[(q0 + o) * kBwdT + cq];  // the centred samples at q
+        if(J.outx) J.outx[(int64_t)y * W + x] = scale * (f.x + 2.0f * v.x * f.z + v.y * f.w);
+        if(J.outy) J.outy[(int64_t)y * W + x] = scale * (f.y + 2.0f * v.y * f.z + v.x * f.w);
+      }
     }
   }
 }
