@@ -19,6 +19,7 @@
 // W*H as the reference does.
 #include <algorithm>
 #include <cfloat>
+#include <type_traits>
 
 #include "qmiv_device.cuh"
 #include "qmiv_ptx.cuh"
@@ -713,6 +714,7 @@ __global__ void __launch_bounds__(256, 3) k_ssim_bwd(const SsimBwdJob* __restric
 {
   using G = BGeo<WIN>;
   constexpr int PW = G::PW, SW = G::SW, VP = G::VP, MP = G::MP, NG = (PW + 7) / 8;
+  static_assert(PW - 32 >= 8 && PW - 32 <= 10, "row groups");
   extern __shared__ __align__(16) float smem[];
   float2* s_in = reinterpret_cast<float2*>(smem);                    // A: [SW][SW] centred a, b
   float4* s_m = reinterpret_cast<float4*>(smem);                     // A: [PW][MP] coefficient maps
@@ -762,24 +764,32 @@ __global__ void __launch_bounds__(256, 3) k_ssim_bwd(const SsimBwdJob* __restric
     }
   }
   __syncthreads();
-  // vertical window sums: thread = staged column q x 8 consecutive p rows
-  for(int it = tid; it < SW * NG; it += 256)
+  // vertical window sums: thread = staged column q x a group of p rows (four groups of 8 and
+  // one of PW - 32), so that the SW x 5 items take one round of the 256 threads at WIN = 10
   {
-    const int q = it % SW, r0 = min(8 * (it / SW), PW - 8);
-    float4 acc[8];
-    #pragma unroll
-    for(int o = 0; o < 8; o++) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
-    #pragma unroll
-    for(int i = 0; i < 7 + WIN; i++)
-    {
-      const float2 ab = s_in[(r0 + i) * SW + q];
-      const float4 v = make_float4(ab.x, ab.y, fmaf(ab.x, ab.x, ab.y * ab.y), ab.x * ab.y);
+    auto vpass = [&](auto nr_tag, int q, int r0) {
+      constexpr int NR = decltype(nr_tag)::value;
+      float4 acc[NR];
       #pragma unroll
-      for(int o = 0; o < 8; o++)
-        if(i - o >= 0 && i - o < WIN) fma4(gk[i - o], v, acc[o]);
+      for(int o = 0; o < NR; o++) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+      #pragma unroll
+      for(int i = 0; i < NR + WIN - 1; i++)
+      {
+        const float2 ab = s_in[(r0 + i) * SW + q];
+        const float4 v = make_float4(ab.x, ab.y, fmaf(ab.x, ab.x, ab.y * ab.y), ab.x * ab.y);
+        #pragma unroll
+        for(int o = 0; o < NR; o++)
+          if(i - o >= 0 && i - o < WIN) fma4(gk[i - o], v, acc[o]);
+      }
+      #pragma unroll
+      for(int o = 0; o < NR; o++) s_v[(r0 + o) * VP + q] = acc[o];
+    };
+    for(int it = tid; it < SW * 5; it += 256)
+    {
+      const int q = it % SW, g = it / SW;
+      if(g < 4) vpass(std::integral_constant<int, 8>{}, q, 8 * g);
+      else      vpass(std::integral_constant<int, PW - 32>{}, q, 32);
     }
-    #pragma unroll
-    for(int o = 0; o < 8; o++) s_v[(r0 + o) * VP + q] = acc[o];
   }
   __syncthreads();
   // horizontal sums -> moments at p -> coefficient maps (zero outside the valid region):
