@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(kCpsTX * kCpsTY) k_loss_cps(Geo g, float w0, f
                                                               int blocks_per_image)
 {
   constexpr int SWX = kCpsTX + 2 * SR, SWY = kCpsTY + 2 * SR;
-  __shared__ float s_t[3][SWY][SWX], s_r[3][SWY][SWX];
+  __shared__ float2 s_rt[3][SWY][SWX];   // (ref, tst) sample pairs: one load feeds both directions
   __shared__ float s_red[8][6];
   const int b = blockIdx.y;
   const int bx = blockIdx.x % ((g.W + kCpsTX - 1) / kCpsTX), by = blockIdx.x / ((g.W + kCpsTX - 1) / kCpsTX);
@@ -121,8 +121,7 @@ __global__ void __launch_bounds__(kCpsTX * kCpsTY) k_loss_cps(Geo g, float w0, f
     {
       const int i = threadIdx.x + kCpsTX * kCpsTY * k;
       if(i >= N) break;
-      (&s_t[0][0][0])[i] = vt[k];
-      (&s_r[0][0][0])[i] = vr[k];
+      (&s_rt[0][0][0])[i] = make_float2(vr[k], vt[k]);
     }
   }
   __syncthreads();
@@ -138,9 +137,11 @@ __global__ void __launch_bounds__(kCpsTX * kCpsTY) k_loss_cps(Geo g, float w0, f
     for(int c = 0; c < 3; c++)
     {
       gc[c] = gcd[b * 3 + c];
-      tg[c] = __fadd_rn(s_t[c][ly + SR][lx + SR], gc[c]);
-      rg[c] = __fsub_rn(s_r[c][ly + SR][lx + SR], gc[c]);
+      tg[c] = __fadd_rn(s_rt[c][ly + SR][lx + SR].y, gc[c]);
+      rg[c] = __fsub_rn(s_rt[c][ly + SR][lx + SR].x, gc[c]);
     }
+    const float2 ntg[3] = { make_float2(-tg[0], -rg[0]), make_float2(-tg[1], -rg[1]), make_float2(-tg[2], -rg[2]) };
+    const float2 wp0 = make_float2(w0, w0), wp1 = make_float2(w1, w1), wp2 = make_float2(w2, w2);
     float best1 = INFINITY, best0 = INFINITY;
     int k1 = 0, k0 = 0;
     #pragma unroll
@@ -151,8 +152,14 @@ __global__ void __launch_bounds__(kCpsTX * kCpsTY) k_loss_cps(Geo g, float w0, f
         // clamped candidate (x+dx-SR, y+dy-SR) in staged coordinates
         const int cx = IN ? lx + dx : min(max(x + dx - SR, 0), g.W - 1) - x0 + SR;
         const int cy = IN ? ly + dy : min(max(y + dy - SR, 0), g.H - 1) - y0 + SR;
-        const float E1 = werr(__fsub_rn(tg[0], s_r[0][cy][cx]), __fsub_rn(tg[1], s_r[1][cy][cx]), __fsub_rn(tg[2], s_r[2][cy][cx]), w0, w1, w2);
-        const float E0 = werr(__fsub_rn(rg[0], s_t[0][cy][cx]), __fsub_rn(rg[1], s_t[1][cy][cx]), __fsub_rn(rg[2], s_t[2][cy][cx]), w0, w1, w2);
+        // both directions in packed FP32: (ref - tg, tst - rg) per component, the negated
+        // differences (their squares are the same), then werr's products and sums lane by lane
+        const float2 d0 = __fadd2_rn(s_rt[0][cy][cx], ntg[0]);
+        const float2 d1 = __fadd2_rn(s_rt[1][cy][cx], ntg[1]);
+        const float2 d2 = __fadd2_rn(s_rt[2][cy][cx], ntg[2]);
+        const float2 E = __fadd2_rn(__fadd2_rn(__fmul2_rn(wp0, __fmul2_rn(d0, d0)), __fmul2_rn(wp1, __fmul2_rn(d1, d1))),
+                                    __fmul2_rn(wp2, __fmul2_rn(d2, d2)));
+        const float E1 = E.x, E0 = E.y;
         const int k = dy * (2 * SR + 1) + dx;
         if(E1 < best1) { best1 = E1; k1 = k; }
         if(E0 < best0) { best0 = E0; k0 = k; }
@@ -168,7 +175,7 @@ __global__ void __launch_bounds__(kCpsTX * kCpsTY) k_loss_cps(Geo g, float w0, f
     float* scp0 = scp + ((int64_t)g.n + b) * 3 * g.plane;
     for(int c = 0; c < 3; c++)
     {
-      const float rv = s_r[c][c1y][c1x], tv = s_t[c][c0y][c0x];
+      const float rv = s_rt[c][c1y][c1x].x, tv = s_rt[c][c0y][c0x].y;
       e1[c] = __fsub_rn(tg[c], rv);
       e0[c] = __fsub_rn(rg[c], tv);
       const float a1 = __fsub_rn(rv, gc[c]), a0 = __fadd_rn(tv, gc[c]);
@@ -332,14 +339,31 @@ __global__ void __launch_bounds__(256) k_loss_grad(BwdArgs a)
     acc[c] = a.g_tst[((int64_t)b * 3 + c) * g.plane + q] + s_f[0][c] * e1 + s_f[2][c];
   }
   // pixels p = q + (dx, dy) whose T2R argmin reads q: those whose stored (clamped) displacement
-  // is (-dx, -dy); the halo's 0xffff never matches
+  // is (-dx, -dy); the halo's 0xffff never matches. The matches are gathered into a bit mask
+  // first and then visited in the same (row-major) order, so that a warp runs the loads of a
+  // neighbour only as many times as its busiest lane has matches, not once per neighbour.
+  constexpr int NW = (side * side + 31) / 32;
+  uint32_t hits[NW];
+  #pragma unroll
+  for(int w = 0; w < NW; w++) hits[w] = 0u;
   #pragma unroll
   for(int dy = -sr; dy <= sr; dy++)
     #pragma unroll
     for(int dx = -sr; dx <= sr; dx++)
+      if((s_m0[ly + kLossMaxSR + dy][lx + kLossMaxSR + dx] & 255) == (sr - dy) * side + (sr - dx))
+      {
+        const int i = (dy + sr) * side + dx + sr;
+        hits[i >> 5] |= 1u << (i & 31);
+      }
+  #pragma unroll
+  for(int w = 0; w < NW; w++)
+  while(hits[w])
+  {
+    const int i = 32 * w + __ffs(hits[w]) - 1;
+    hits[w] &= hits[w] - 1;
     {
+      const int dy = i / side - sr, dx = i - (i / side) * side - sr;
       const int m0 = s_m0[ly + kLossMaxSR + dy][lx + kLossMaxSR + dx];
-      if((m0 & 255) != (sr - dy) * side + (sr - dx)) continue;
       const int px = x + dx, py = y + dy;
       const int64_t p = (int64_t)py * g.W + px;
       #pragma unroll
@@ -351,6 +375,7 @@ __global__ void __launch_bounds__(256) k_loss_grad(BwdArgs a)
         acc[c] += v;
       }
     }
+  }
   #pragma unroll
   for(int c = 0; c < 3; c++) a.g_tst[((int64_t)b * 3 + c) * g.plane + q] = acc[c];
 }
