@@ -393,8 +393,9 @@ template <int SR, int QPW, int NWD, typename KeyT, typename T>
 cudaError_t launch_tma(const DevJob* d, int n, int blocks, const Params& p, cudaStream_t st)
 {
   using G = TGeo<SR, QPW, NWD, T, KeyT>;
-  static bool attr = false;
-  if(!attr)
+  static std::atomic<bool> attr[kStaticMaxDevices];
+  const int dv = device_slot();
+  if(!attr[dv].load(std::memory_order_acquire))
   {
     cudaError_t e = cudaFuncSetAttribute(k_cps420_tma<SR, QPW, NWD, KeyT, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM);
     if(e != cudaSuccess) return e;
@@ -402,7 +403,7 @@ cudaError_t launch_tma(const DevJob* d, int n, int blocks, const Params& p, cuda
     // global data through L1, and the default split held it to two resident blocks
     e = cudaFuncSetAttribute(k_cps420_tma<SR, QPW, NWD, KeyT, T>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if(e != cudaSuccess) return e;
-    attr = true;
+    attr[dv].store(true, std::memory_order_release);
   }
   k_cps420_tma<SR, QPW, NWD, KeyT, T><<<blocks, G::NT, G::SMEM, st>>>(d, n, p);
   return cudaGetLastError();

@@ -925,23 +925,23 @@ cudaError_t launch_ssim(const SsimJob* d_jobs, const SsimJob* h_jobs, int n, int
   for(int i = 0; i < n; i++) tiles = h_jobs[i].tile_base + h_jobs[i].tiles_x * h_jobs[i].tiles_y;
   if(tiles > 0)
   {
-    static int resident[2] = { 0, 0 };  // blocks per SM, per window
-    static int sms = 0;
-    const int wi = window == QMIV_SSIM_GAUSS11 ? 1 : 0;
-    if(!resident[wi])
+    static std::atomic<int> resident[kStaticMaxDevices][2];  // blocks per SM x SMs, per device and window
+    const int wi = window == QMIV_SSIM_GAUSS11 ? 1 : 0, dv = device_slot();
+    int slots = resident[dv][wi].load(std::memory_order_acquire);
+    if(!slots)
     {
-      int dev = 0;
-      cudaError_t e = cudaGetDevice(&dev);
-      if(e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      int sms = 0, r = 0;
+      cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dv);
       if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, SGeo<10>::SMEM);
       if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim<11>, cudaFuncAttributeMaxDynamicSharedMemorySize, SGeo<11>::SMEM);
       if(e == cudaSuccess)
-        e = wi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[1], k_ssim<11>, kThreads, SGeo<11>::SMEM)
-               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[0], k_ssim<10>, kThreads, SGeo<10>::SMEM);
+        e = wi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_ssim<11>, kThreads, SGeo<11>::SMEM)
+               : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_ssim<10>, kThreads, SGeo<10>::SMEM);
       if(e != cudaSuccess) return e;
-      if(resident[wi] < 1) resident[wi] = 1;
+      slots = std::max(1, r) * std::max(1, sms);
+      resident[dv][wi].store(slots, std::memory_order_release);
     }
-    const int grid = std::min(tiles, sms * resident[wi]);
+    const int grid = std::min(tiles, slots);
     if(wi) k_ssim<11><<<grid, kThreads, SGeo<11>::SMEM, st>>>(d_jobs, n, tiles);
     else   k_ssim<10><<<grid, kThreads, SGeo<10>::SMEM, st>>>(d_jobs, n, tiles);
     cudaError_t e = cudaGetLastError();
@@ -958,8 +958,9 @@ cudaError_t launch_ssim_bwd(const SsimBwdJob* d_jobs, const SsimBwdJob* h_jobs, 
   int blocks = 0;
   for(int i = 0; i < n; i++) blocks = h_jobs[i].tile_base + h_jobs[i].tiles_x * h_jobs[i].tiles_y;
   if(blocks == 0) return cudaSuccess;
-  static bool attr = false;
-  if(!attr)
+  static std::atomic<bool> attr[kStaticMaxDevices];
+  const int dv = device_slot();
+  if(!attr[dv].load(std::memory_order_acquire))
   {
     cudaError_t e = cudaFuncSetAttribute(k_ssim_bwd<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, BGeo<10>::SMEM);
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_bwd<11>, cudaFuncAttributeMaxDynamicSharedMemorySize, BGeo<11>::SMEM);
@@ -967,7 +968,7 @@ cudaError_t launch_ssim_bwd(const SsimBwdJob* d_jobs, const SsimBwdJob* h_jobs, 
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_bwd<10>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_bwd<11>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if(e != cudaSuccess) return e;
-    attr = true;
+    attr[dv].store(true, std::memory_order_release);
   }
   if(window == QMIV_SSIM_GAUSS11) k_ssim_bwd<11><<<blocks, 256, BGeo<11>::SMEM, st>>>(d_jobs, n);
   else                            k_ssim_bwd<10><<<blocks, 256, BGeo<10>::SMEM, st>>>(d_jobs, n);
@@ -981,26 +982,26 @@ cudaError_t launch_ssim_quad(const SsimQuadJob* d_jobs, const SsimQuadJob* h_job
   int tiles = 0;
   for(int i = 0; i < n; i++) tiles = h_jobs[i].tile_base + h_jobs[i].tiles_x * h_jobs[i].tiles_y;
   if(tiles == 0) return cudaSuccess;
-  static int resident[2] = { 0, 0 };
-  static int sms = 0;
-  const int wi = window == QMIV_SSIM_GAUSS11 ? 1 : 0;
-  if(!resident[wi])
+  static std::atomic<int> resident[kStaticMaxDevices][2];  // blocks per SM x SMs, per device and window
+  const int wi = window == QMIV_SSIM_GAUSS11 ? 1 : 0, dv = device_slot();
+  int slots = resident[dv][wi].load(std::memory_order_acquire);
+  if(!slots)
   {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if(e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int sms = 0, r = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dv);
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_quad<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, QGeo<10>::SMEM);
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_quad<11>, cudaFuncAttributeMaxDynamicSharedMemorySize, QGeo<11>::SMEM);
     // three resident blocks need nearly all of the unified L1 as shared memory
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_quad<10>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_quad<11>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if(e == cudaSuccess)
-      e = wi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[1], k_ssim_quad<11>, kThreads, QGeo<11>::SMEM)
-             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident[0], k_ssim_quad<10>, kThreads, QGeo<10>::SMEM);
+      e = wi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_ssim_quad<11>, kThreads, QGeo<11>::SMEM)
+             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_ssim_quad<10>, kThreads, QGeo<10>::SMEM);
     if(e != cudaSuccess) return e;
-    if(resident[wi] < 1) resident[wi] = 1;
+    slots = std::max(1, r) * std::max(1, sms);
+    resident[dv][wi].store(slots, std::memory_order_release);
   }
-  const int grid = std::min(tiles, sms * resident[wi]);
+  const int grid = std::min(tiles, slots);
   if(wi) k_ssim_quad<11><<<grid, kThreads, QGeo<11>::SMEM, st>>>(d_jobs, n, tiles);
   else   k_ssim_quad<10><<<grid, kThreads, QGeo<10>::SMEM, st>>>(d_jobs, n, tiles);
   return cudaGetLastError();

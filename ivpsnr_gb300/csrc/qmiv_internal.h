@@ -1,5 +1,6 @@
 // Internal device-side descriptors shared by the kernels and the host launcher.
 #pragma once
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -68,6 +69,15 @@ cudaError_t launch_stats(const DevJob* d_jobs, const DevJob* h_jobs, int n, cons
 // Statistics of one picture pair in a static device array (k_stats.cu): no allocation.
 constexpr int kStaticMaxRows = 8192;     // tallest picture the static row sums hold
 constexpr int kStaticMaxDevices = 64;
+
+// Launch attributes (cudaFuncSetAttribute, occupancy) belong to the current device, so the
+// launchers keep their one-time set-up per device ordinal.
+inline int device_slot()
+{
+  int d = 0;
+  if(cudaGetDevice(&d) != cudaSuccess || d < 0 || d >= kStaticMaxDevices) d = 0;
+  return d;
+}
 struct StaticStatsScratch {
   int64_t* stat_rows;                    // [kStaticMaxRows][6]
   JobScalars* sc;                        // stats_done must be 0 when the kernel starts
