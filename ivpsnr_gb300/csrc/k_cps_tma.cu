@@ -134,7 +134,46 @@ k_cps420_tma(const DevJob* __restrict__ jobs, int njobs, Params p)
     {
       const bool border = (y0 - SR < 0) || (y0 + G::R + SR > H) || (cx0 - SR < 0) || (cx0 + 64 + SR > W);
       constexpr int PAIRS = G::TW / 2;
-      for(int idx = tid; idx < 2 * G::TH * PAIRS; idx += G::NT)
+      bool done = false;
+      if constexpr(CE == 2 && G::TW % 4 == 0)
+      {
+        if(!border)
+        { // interior chunk, (sample, square) tile: four samples per item from two 2-sample
+          // words, the scale as a shift when it is a power of two
+          constexpr int QUADS = G::TW / 4;
+          using W2 = typename std::conditional<sizeof(T) == 2, uint32_t, uint16_t>::type;
+          constexpr int WB = 8 * (int)sizeof(T);
+          const int ls = p.luma_scale_log2;
+          constexpr int ITEMS = 2 * G::TH * QUADS, PER = (ITEMS + G::NT - 1) / G::NT;
+          constexpr unsigned M = (1u << WB) - 1u;
+          W2 w[PER][2];
+          #pragma unroll
+          for(int k = 0; k < PER; k++)
+          { // every load first
+            const int idx = min(tid + k * G::NT, ITEMS - 1);
+            const int row = idx / QUADS, qd = idx - row * QUADS;  // row = picture * TH + staged row
+            const int pic = row >= G::TH ? 1 : 0, ty = row - pic * G::TH;
+            const T* rl = reinterpret_cast<const T*>(sb + pic * G::LBOX) + ty * G::RW + 4 * qd + G::XA - SR;
+            w[k][0] = *reinterpret_cast<const W2*>(rl);
+            w[k][1] = *reinterpret_cast<const W2*>(rl + 2);
+          }
+          #pragma unroll
+          for(int k = 0; k < PER; k++)
+          {
+            const int idx = tid + k * G::NT;
+            if(idx >= ITEMS) break;
+            const int row = idx / QUADS, qd = idx - row * QUADS;
+            int v[4] = { (int)(w[k][0] & M), (int)(w[k][0] >> WB), (int)(w[k][1] & M), (int)(w[k][1] >> WB) };
+            #pragma unroll
+            for(int j = 0; j < 4; j++) v[j] = ls >= 0 ? v[j] << ls : s * v[j];
+            int* dst = &cvt[2 * (row * G::TW + 4 * qd)];
+            *reinterpret_cast<int4*>(dst) = make_int4(v[0], v[0] * v[0], v[1], v[1] * v[1]);
+            *reinterpret_cast<int4*>(dst + 4) = make_int4(v[2], v[2] * v[2], v[3], v[3] * v[3]);
+          }
+          done = true;
+        }
+      }
+      for(int idx = tid; !done && idx < 2 * G::TH * PAIRS; idx += G::NT)
       {
         const int pic = idx / (G::TH * PAIRS);
         const int rem = idx - pic * (G::TH * PAIRS);
