@@ -459,6 +459,9 @@ const CpsVariant kVariants[] = {
   VT(1, 4, 4, unsigned int, uint16_t, false, 2, "_k32_u16"),
   VT(3, 4, 4, unsigned int, uint16_t, false, 2, "_k32_u16"),
   VT(4, 4, 4, unsigned int, uint16_t, false, 2, "_k32_u16"),
+  VT(1, 4, 2, unsigned int, uint16_t, false, 2, "_k32_u16"),
+  VT(3, 4, 2, unsigned int, uint16_t, false, 2, "_k32_u16"),
+  VT(4, 4, 2, unsigned int, uint16_t, false, 2, "_k32_u16"),
   VT(1, 4, 4, unsigned long long, uint16_t, true, 2, "_k64_u16"),
   VT(2, 4, 4, unsigned long long, uint16_t, true, 2, "_k64_u16"),
   VT(3, 4, 4, unsigned long long, uint16_t, true, 2, "_k64_u16"),

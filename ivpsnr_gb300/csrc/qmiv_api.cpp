@@ -254,9 +254,12 @@ int pick_cps_variant(const qmiv_handle* h, const DevJob& j)
   if(!j.cshift || h->opt.cmp_w_search[0] < 1 || sr < 1 || sr > 4) return 0; // generic
   if(h->cps_variant_override == 0) return 0;
   if(cps_variant_fits(h, j, h->cps_variant_override)) return h->cps_variant_override;
-  // default: the TMA kernel with 16-row strips and 4 warps (more resident blocks), else the
-  // one with 32-row strips and 8 warps, else the staged-load kernel
-  for(const char* shape : { "_q4_w2", "_q4_w4" })
+  // default: at search range <= 2 the TMA kernel with 16-row strips and 4 warps (more resident
+  // blocks), above it the one with 32-row strips and 8 warps (measured faster at range 4 on
+  // 8K frames); else the staged-load kernel
+  const char* first = sr <= 2 ? "_q4_w2" : "_q4_w4";
+  const char* second = sr <= 2 ? "_q4_w4" : "_q4_w2";
+  for(const char* shape : { first, second })
     for(int v = 1; v < (int)V.size(); v++)
       if(cps_variant_fits(h, j, v) && V[v].kind == 2 && std::strstr(V[v].name, shape)) return v;
   for(int v = 1; v < (int)V.size(); v++)
