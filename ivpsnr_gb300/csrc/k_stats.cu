@@ -22,6 +22,26 @@ namespace {
 constexpr int kStatsThreads = 256;
 constexpr int kRowPairsPerBlock = kStatsThreads / 32; // one warp per pair of luma rows
 
+// Differences of the samples packed in two 32-bit words (2 x 16-bit or 4 x 8-bit): their sum
+// into sd, the sum of their squares into q. Lanes are taken out with shifts and masks, so the
+// loaded vectors stay in registers.
+template <typename T>
+__device__ __forceinline__ void word_stats(uint32_t a, uint32_t b, int& sd, unsigned int& q)
+{
+  if(sizeof(T) == 2)
+  {
+    const int d0 = (int)(a & 0xFFFFu) - (int)(b & 0xFFFFu), d1 = (int)(a >> 16) - (int)(b >> 16);
+    sd += d0 + d1;
+    q += (unsigned)(d0 * d0) + (unsigned)(d1 * d1);
+  }
+  else
+  { // sum of |d|^2 as a byte dot product of the absolute differences with themselves
+    const unsigned ad = __vabsdiffu4(a, b);
+    q = __dp4a(ad, ad, q);
+    sd += (int)__dp4a(a, 0x01010101u, 0u) - (int)__dp4a(b, 0x01010101u, 0u);
+  }
+}
+
 // sum(a-b) and sum((a-b)^2) over n samples of two rows, one warp, 16-byte loads when aligned
 template <typename T>
 __device__ __forceinline__ void row_stats(const T* __restrict__ a, const T* __restrict__ b, int n, bool vec, int lane,
@@ -38,11 +58,11 @@ __device__ __forceinline__ void row_stats(const T* __restrict__ a, const T* __re
     for(int i = lane; i < nv; i += 32)
     {
       const uint4 x = __ldg(av + i), y = __ldg(bv + i);
-      const T* xs = reinterpret_cast<const T*>(&x);
-      const T* ys = reinterpret_cast<const T*>(&y);
       unsigned int q = 0;
-      #pragma unroll
-      for(int k = 0; k < V; k++) { const int d = (int)xs[k] - (int)ys[k]; sd += d; q += (unsigned int)(d * d); }
+      word_stats<T>(x.x, y.x, sd, q);
+      word_stats<T>(x.y, y.y, sd, q);
+      word_stats<T>(x.z, y.z, sd, q);
+      word_stats<T>(x.w, y.w, sd, q);
       ssd += q;
     }
     i0 = nv * V;
@@ -55,29 +75,32 @@ __device__ __forceinline__ void row_stats(const T* __restrict__ a, const T* __re
 }
 
 template <typename T>
-__device__ void stats_rowpair(const DevJob& J, int y, bool vec, int lane, int sd[2][3], unsigned long long ssd[2][3])
-{
-  const T* p0[3]; const T* p1[3];
-  for(int c = 0; c < 3; c++) { p0[c] = (const T*)J.p0[c]; p1[c] = (const T*)J.p1[c]; }
+__device__ __forceinline__ void stats_rowpair(const DevJob& J, int y, bool vec, int lane, int (&sd)[2][3],
+                                              unsigned long long (&ssd)[2][3])
+{ // every loop unrolled, so that the accumulators stay in registers
+  const bool two = y + 1 < J.H;
+  #pragma unroll
   for(int r = 0; r < 2; r++)
-  {
-    if(y + r >= J.H) break;
-    row_stats<T>(p1[0] + (int64_t)(y + r) * J.stride1[0], p0[0] + (int64_t)(y + r) * J.stride0[0], J.W, vec, lane, sd[r][0], ssd[r][0]);
-  }
+    if(r == 0 || two)
+      row_stats<T>((const T*)J.p1[0] + (int64_t)(y + r) * J.stride1[0], (const T*)J.p0[0] + (int64_t)(y + r) * J.stride0[0],
+                   J.W, vec, lane, sd[r][0], ssd[r][0]);
   if(J.cshift)
   { // one chroma row serves luma rows y and y+1
     const int cy = y >> 1, cw = J.W >> 1;
+    #pragma unroll
     for(int c = 1; c < 3; c++)
-      row_stats<T>(p1[c] + (int64_t)cy * J.stride1[c], p0[c] + (int64_t)cy * J.stride0[c], cw, vec, lane, sd[0][c], ssd[0][c]);
+      row_stats<T>((const T*)J.p1[c] + (int64_t)cy * J.stride1[c], (const T*)J.p0[c] + (int64_t)cy * J.stride0[c], cw, vec,
+                   lane, sd[0][c], ssd[0][c]);
   }
   else
   {
+    #pragma unroll
     for(int r = 0; r < 2; r++)
-    {
-      if(y + r >= J.H) break;
+      #pragma unroll
       for(int c = 1; c < 3; c++)
-        row_stats<T>(p1[c] + (int64_t)(y + r) * J.stride1[c], p0[c] + (int64_t)(y + r) * J.stride0[c], J.W, vec, lane, sd[r][c], ssd[r][c]);
-    }
+        if(r == 0 || two)
+          row_stats<T>((const T*)J.p1[c] + (int64_t)(y + r) * J.stride1[c], (const T*)J.p0[c] + (int64_t)(y + r) * J.stride0[c],
+                       J.W, vec, lane, sd[r][c], ssd[r][c]);
   }
 }
 
