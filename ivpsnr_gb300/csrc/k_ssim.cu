@@ -620,16 +620,28 @@ __global__ void __launch_bounds__(256) k_ssim_finalize(const SsimJob* __restrict
 }
 
 // DownsampleHV to a 16-bit plane: d(x,y) = (s(2x,2y)+s(2x+1,2y)+s(2x,2y+1)+s(2x+1,2y+1)+2)>>2
+// Grid: x = 64-column groups, y = groups of kDownRows output rows, z = steps; a thread makes
+// kDownRows / 4 outputs of one column, all loads issued before the stores.
+constexpr int kDownRows = 16;
 __global__ void __launch_bounds__(256) k_downsample(const PyrStep* __restrict__ steps, int nsteps)
 {
-  const PyrStep& S = steps[blockIdx.y];
+  const PyrStep& S = steps[blockIdx.z];
   const int x = blockIdx.x * 64 + (threadIdx.x & 63);
-  for(int y = threadIdx.x >> 6; y < S.dh; y += 4)
+  const int y0 = blockIdx.y * kDownRows + (threadIdx.x >> 6);
+  if(x >= S.dw || y0 >= S.dh) return;
+  constexpr int K = kDownRows / 4;
+  int v[K];
+  #pragma unroll
+  for(int k = 0; k < K; k++)
   {
-    if(x >= S.dw) break;
-    const int sx = 2 * x, sy = 2 * y;
-    const int v = ld_int(S.src, sx, sy) + ld_int(S.src, sx + 1, sy) + ld_int(S.src, sx, sy + 1) + ld_int(S.src, sx + 1, sy + 1);
-    S.dst[(int64_t)y * S.dst_stride + x] = (uint16_t)((v + 2) >> 2);
+    const int sx = 2 * x, sy = 2 * min(y0 + 4 * k, S.dh - 1);
+    v[k] = ld_int(S.src, sx, sy) + ld_int(S.src, sx + 1, sy) + ld_int(S.src, sx, sy + 1) + ld_int(S.src, sx + 1, sy + 1);
+  }
+  #pragma unroll
+  for(int k = 0; k < K; k++)
+  {
+    const int y = y0 + 4 * k;
+    if(y < S.dh) S.dst[(int64_t)y * S.dst_stride + x] = (uint16_t)((v[k] + 2) >> 2);
   }
 }
 
@@ -1009,10 +1021,10 @@ cudaError_t launch_ssim_quad(const SsimQuadJob* d_jobs, const SsimQuadJob* h_job
 
 cudaError_t launch_downsample(const PyrStep* d_steps, const PyrStep* h_steps, int n, cudaStream_t st)
 {
-  int maxw = 0;
-  for(int i = 0; i < n; i++) maxw = h_steps[i].dw > maxw ? h_steps[i].dw : maxw;
-  if(n == 0 || maxw == 0) return cudaSuccess;
-  dim3 grid((maxw + 63) / 64, n);
+  int maxw = 0, maxh = 0;
+  for(int i = 0; i < n; i++) { maxw = std::max(maxw, h_steps[i].dw); maxh = std::max(maxh, h_steps[i].dh); }
+  if(n == 0 || maxw == 0 || maxh == 0) return cudaSuccess;
+  dim3 grid((maxw + 63) / 64, (maxh + kDownRows - 1) / kDownRows, n);
   k_downsample<<<grid, 256, 0, st>>>(d_steps, n);
   return cudaGetLastError();
 }
