@@ -601,19 +601,36 @@ __global__ void __launch_bounds__(kThreads, 3) k_ssim_quad(const SsimQuadJob* __
   }
 }
 
-// Picture sum of one SSIM job: rows summed over their tiles in FP64 (fixed order), rows combined
-// with a compensated sum, divided by W*H (xSSIM.cpp:106-111).
-__global__ void __launch_bounds__(256) k_ssim_finalize(const SsimJob* __restrict__ jobs, int njobs)
+// Picture sum of one SSIM job (xSSIM.cpp:106-111): a thread per row adds the row's per-tile sums
+// in order as an exact FP32 pair (TwoSum), the row value goes to FP64 once, rows are combined
+// with a compensated sum in a fixed order, and the picture sum is divided by W*H. FP32 pairs
+// rather than FP64 adds per tile: GB300's FP64 rate made the per-tile adds the cost of this
+// kernel on large pictures.
+__device__ __forceinline__ void fin_two_sum(float a, float b, float& s, float& e)
 {
-  __shared__ double scratch[16];
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+constexpr int kFinThreads = 512;
+__global__ void __launch_bounds__(kFinThreads) k_ssim_finalize(const SsimJob* __restrict__ jobs, int njobs)
+{
+  __shared__ double scratch[2 * (kFinThreads / 32)];
   const SsimJob& J = jobs[blockIdx.x];
   const int rows = max(0, J.H - 10);
   Kbns k = { 0.0, 0.0 };
-  for(int r = threadIdx.x; r < rows; r += blockDim.x)
+  for(int r = threadIdx.x; r < rows; r += kFinThreads)
   {
-    double s = 0.0;
-    for(int t = 0; t < J.tiles_x; t++) s = __dadd_rn(s, (double)__ldcg(J.partial + (int64_t)r * J.tiles_x + t));
-    k = kbns_add(k, s);
+    const float* pr = J.partial + (int64_t)r * J.tiles_x;
+    float hi = 0.0f, lo = 0.0f;
+    for(int t = 0; t < J.tiles_x; t++)
+    {
+      float e;
+      fin_two_sum(hi, __ldcg(pr + t), hi, e);
+      lo = __fadd_rn(lo, e);
+    }
+    k = kbns_add(k, __dadd_rn((double)hi, (double)lo));
   }
   const double tot = block_kbns(k, scratch);
   if(threadIdx.x == 0) *J.out = __ddiv_rn(tot, (double)((int64_t)J.W * J.H));
@@ -959,7 +976,7 @@ cudaError_t launch_ssim(const SsimJob* d_jobs, const SsimJob* h_jobs, int n, int
     cudaError_t e = cudaGetLastError();
     if(e != cudaSuccess) return e;
   }
-  k_ssim_finalize<<<n, 256, 0, st>>>(d_jobs, n);
+  k_ssim_finalize<<<n, kFinThreads, 0, st>>>(d_jobs, n);
   return cudaGetLastError();
 }
 
