@@ -324,6 +324,109 @@ def stream_workload(args, dev):
                       "msssim_frame0": list(r0.msssim)[:3]}}
 
 
+def ellipse_mask(w, h, seed):
+    """8-bit mask, 255 outside four seeded ellipses and 0 inside (the masked workload's mask)."""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:h, 0:w].astype(np.float32)
+    m = np.full((h, w), 255, np.uint8)
+    for _ in range(4):
+        cx, cy = rng.uniform(0, w), rng.uniform(0, h)
+        ax, ay = rng.uniform(0.05, 0.25) * w, rng.uniform(0.05, 0.25) * h
+        m[((x - cx) / ax) ** 2 + ((y - cy) / ay) ** 2 <= 1.0] = 0
+    return m
+
+
+def next_rows_workload(args, dev):
+    """The calls beside the metric path, each on device-resident inputs unless stated:
+    masked IV-PSNR/PSNR/WS-PSNR/GCD on 1920x1080 10-bit 4:2:0 (qmiv_calc_frame_masked), the raw
+    YUV reader (qmiv_yuv_read of a 10-bit 4:2:0 1920x1080 file in the page cache, host read and
+    upload included), the range check (qmiv_check_range, counting only) and the colour conversion
+    (qmiv_color_convert) on 4096x2048 10-bit pictures. HBM-bound calls are also given as a
+    fraction of the measured copy bandwidth."""
+    import ctypes as C
+    import tempfile
+
+    import torch
+
+    import ivpsnr_gb300 as q
+    from ivpsnr_gb300 import _abi, synth
+    lib = _abi.load()
+    hbm, kind = peaks()
+    reps = max(3, args.steps)
+    out = {}
+
+    def timed(fn, n):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(n):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n
+
+    # masked metrics
+    w, h = 1920, 1080
+    ref, tst = synth.pair420(w, h, BD, seed=synth.seed_for(5, 0, 0), holes=True)
+    pl = lambda flat: [torch.from_numpy(np.ascontiguousarray(p.astype(np.uint16)).view(np.int16)).to(dev)
+                       for p in synth.split420(flat, w, h)]
+    d0, d1 = pl(ref), pl(tst)
+    mask = torch.from_numpy(ellipse_mask(w, h, 5)).to(dev)
+    with q.Processor(w, h) as P:
+        p0, p1 = q.make_pic(d0, BD), q.make_pic(d1, BD)
+        ms = timed(lambda: P.calc_frame_masked(p0, p1, mask, 8), reps)
+    out["masked"] = {"call": "qmiv_calc_frame_masked", "picture": "1920x1080 10-bit 4:2:0, ellipse mask",
+                     "ms": ms, "value": w * h / (ms * 1e-3) / 1e9, "unit": "Gpixel/s"}
+
+    # raw YUV reader: eight frames of 10-bit 4:2:0, read in turn
+    nf = 8
+    fb = w * h * 3 // 2 * 2
+    with tempfile.NamedTemporaryFile(suffix=".yuv", delete=False) as fh:
+        path = fh.name
+        for f in range(nf):
+            r, _ = synth.pair420(w, h, BD, seed=synth.seed_for(5, 1, f))
+            fh.write(r.astype("<u2").tobytes())
+    try:
+        rd = C.c_void_p()
+        _abi.check(lib.qmiv_yuv_open(C.byref(rd), path.encode(), w, h, BD, 420), "qmiv_yuv_open")
+        pic = _abi.Pic()
+        k = [0]
+
+        def read_one():
+            _abi.check(lib.qmiv_yuv_read(rd, k[0] % nf, C.byref(pic), None), "qmiv_yuv_read")
+            k[0] += 1
+        ms = timed(read_one, 4 * nf)
+        lib.qmiv_yuv_close(rd)
+    finally:
+        os.unlink(path)
+    out["yuv_read"] = {"call": "qmiv_yuv_read", "picture": "1920x1080 10-bit 4:2:0 frames from the page cache",
+                       "ms": ms, "value": w * h / (ms * 1e-3) / 1e9, "unit": "Gpixel/s",
+                       "gbs": fb / (ms * 1e-3) / 1e9}
+
+    # range check and colour conversion on 4096x2048 4:4:4 10-bit
+    W, H = 4096, 2048
+    g = torch.Generator(device="cpu").manual_seed(7)
+    planes = [torch.randint(0, 1 << BD, (H, W), generator=g, dtype=torch.int16).to(dev) for _ in range(3)]
+    pic = q.make_pic(planes, BD, q.CF444)
+    cnt = (C.c_int64 * 3)()
+    ms = timed(lambda: _abi.check(lib.qmiv_check_range(C.byref(pic), 0, cnt, None), "qmiv_check_range"), reps)
+    nbytes = 3 * W * H * 2
+    out["range_check"] = {"call": "qmiv_check_range (count only, synchronous)", "picture": "4096x2048 10-bit 4:4:4",
+                          "ms": ms, "gbs": nbytes / (ms * 1e-3) / 1e9, "frac_of_hbm": nbytes / (ms * 1e-3) / 1e9 / hbm,
+                          "peak_kind": kind}
+    dst = [torch.empty((H, W), dtype=torch.int16, device=dev) for _ in range(3)]
+    dptr = (C.c_void_p * 3)(*[t.data_ptr() for t in dst])
+    ms = timed(lambda: _abi.check(lib.qmiv_color_convert(C.byref(pic), dptr, W, 1, 1, None), "qmiv_color_convert"), reps)
+    out["color_convert"] = {"call": "qmiv_color_convert (RGB to YCbCr, BT.709)", "picture": "4096x2048 10-bit 4:4:4",
+                            "ms": ms, "gbs": 2 * nbytes / (ms * 1e-3) / 1e9,
+                            "frac_of_hbm": 2 * nbytes / (ms * 1e-3) / 1e9 / hbm, "peak_kind": kind}
+    del planes, dst, d0, d1, mask
+    torch.cuda.empty_cache()
+    return out
+
+
 LOSS_WORKLOAD = ("ivssim-ivpsnr-loss-fwd-bwd: 16 x FP32 4:4:4 1024x1024 in [0,1], tested = reference + N(0, 0.02^2)"
                  " + per-channel offset + block shifts, SR 2, REF10 window")
 
@@ -600,6 +703,7 @@ def run_ours(args):
     ssim_line = None if args.skip_ssim else ssim_workload(args, dev, stream)
     loss_line = None if args.skip_loss else loss_workload(args, dev)
     stream_line = None if args.skip_stream else stream_workload(args, dev)
+    next_line = None if args.skip_next else next_rows_workload(args, dev)
 
     if rank == 0:
         line = {
@@ -632,6 +736,8 @@ def run_ours(args):
             line["loss"] = loss_line
         if stream_line:
             line["stream"] = stream_line
+        if next_line:
+            line["next_rows"] = next_line
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline_sample()
         print(json.dumps(line))
@@ -651,6 +757,8 @@ def main():
     ap.add_argument("--skip-ssim", action="store_true", help="skip the IV-SSIM / SSIM / MS-SSIM workload")
     ap.add_argument("--skip-loss", action="store_true", help="skip the differentiable-loss forward/backward workload")
     ap.add_argument("--skip-stream", action="store_true", help="skip the streamed 8K ERP sequence workload")
+    ap.add_argument("--skip-next", action="store_true",
+                    help="skip the masked / YUV reader / range check / colour conversion measurements")
     ap.add_argument("--kernels-only", action="store_true",
                     help="time only the batched launches (for profiler captures)")
     args = ap.parse_args()

@@ -33,27 +33,58 @@ __global__ void k_upsample_h(const void* __restrict__ src, int sbytes, int sstri
   else            ((uint16_t*)dst)[(int64_t)y * W + x] = (uint16_t)v;
 }
 
-// count samples above Max in one plane; optionally clip them in place
+// count samples above Max in one plane; optionally clip them in place. A block walks rows
+// (grid-stride over rows, threads over columns), 16-bit rows in 8-sample vectors when the row
+// starts on 16 bytes, so no 64-bit division per sample.
+__device__ __forceinline__ unsigned range_word(uint32_t& w, int maxv, int conceal)
+{ // two 16-bit samples
+  const int lo = (int)(w & 0xFFFFu), hi = (int)(w >> 16);
+  const unsigned n = (unsigned)(lo > maxv) + (unsigned)(hi > maxv);
+  if(conceal && n) w = (uint32_t)min(lo, maxv) | ((uint32_t)min(hi, maxv) << 16);
+  return n;
+}
+
 __global__ void __launch_bounds__(256) k_range(void* plane, int sbytes, int stride, int w, int h, int maxv, int conceal,
                                                unsigned long long* count)
 {
   __shared__ unsigned int s_n[8];
   unsigned int n = 0;
-  const int64_t total = (int64_t)w * h;
-  for(int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x)
+  const bool vec = sbytes == 2 && ((((uintptr_t)plane) | ((size_t)stride * 2)) & 15) == 0;
+  for(int y = blockIdx.x; y < h; y += gridDim.x)
   {
-    const int y = (int)(i / w), x = (int)(i - (int64_t)y * w);
-    const int64_t o = (int64_t)y * stride + x;
-    const int v = ld_rw(plane, sbytes, o);
-    if(v > maxv)
+    if(vec)
     {
-      n++;
-      if(conceal)
+      uint4* row = reinterpret_cast<uint4*>((uint16_t*)plane + (int64_t)y * stride);
+      const int nv = w >> 3;
+      for(int i = threadIdx.x; i < nv; i += blockDim.x)
       {
-        if(sbytes == 1) ((uint8_t*)plane)[o] = (uint8_t)maxv;
-        else            ((uint16_t*)plane)[o] = (uint16_t)maxv;
+        uint4 v = row[i];
+        const unsigned c = range_word(v.x, maxv, conceal) + range_word(v.y, maxv, conceal) +
+                           range_word(v.z, maxv, conceal) + range_word(v.w, maxv, conceal);
+        n += c;
+        if(conceal && c) row[i] = v;
+      }
+      for(int x = 8 * nv + threadIdx.x; x < w; x += blockDim.x)
+      {
+        uint16_t* p = (uint16_t*)plane + (int64_t)y * stride + x;
+        if((int)*p > maxv) { n++; if(conceal) *p = (uint16_t)maxv; }
       }
     }
+    else
+      for(int x = threadIdx.x; x < w; x += blockDim.x)
+      {
+        const int64_t o = (int64_t)y * stride + x;
+        const int v = ld_rw(plane, sbytes, o);
+        if(v > maxv)
+        {
+          n++;
+          if(conceal)
+          {
+            if(sbytes == 1) ((uint8_t*)plane)[o] = (uint8_t)maxv;
+            else            ((uint16_t*)plane)[o] = (uint16_t)maxv;
+          }
+        }
+      }
   }
   for(int d = 16; d > 0; d >>= 1) n += __shfl_xor_sync(0xffffffffu, n, d);
   if((threadIdx.x & 31) == 0) s_n[threadIdx.x >> 5] = n;
@@ -68,14 +99,9 @@ __global__ void __launch_bounds__(256) k_range(void* plane, int sbytes, int stri
 
 __device__ __forceinline__ int clipu(int v, int mx) { return v < 0 ? 0 : (v > mx ? mx : v); }
 
-__global__ void k_color(ColorJob J)
+__device__ __forceinline__ void color_px(const ColorJob& J, int a, int b, int c, int& o0, int& o1, int& o2)
 {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
-  if(x >= J.W || y >= J.H) return;
-  const int64_t so = (int64_t)y * J.sstride + x, dof = (int64_t)y * J.dstride + x;
-  const int a = ld_rw(J.src[0], J.sbytes, so), b = ld_rw(J.src[1], J.sbytes, so), c = ld_rw(J.src[2], J.sbytes, so);
   const int mid = 1 << (J.bd - 1), mx = (1 << J.bd) - 1;
-  int o0, o1, o2;
   if(J.to_ycbcr)
   { // a, b, c = R, G, B (xColorSpaceSTD.cpp:195-232)
     const int ty = (J.m[0][0] * a + J.m[0][1] * b + J.m[0][2] * c + kColorAdd) >> kColorPrec;
@@ -91,9 +117,47 @@ __global__ void k_color(ColorJob J)
     o1 = clipu((sy + J.m[1][1] * iu + J.m[1][2] * iv) >> kColorPrec, mx);
     o2 = clipu((sy + J.m[2][1] * iu) >> kColorPrec, mx);
   }
-  J.dst[0][dof] = (uint16_t)o0;
-  J.dst[1][dof] = (uint16_t)o1;
-  J.dst[2][dof] = (uint16_t)o2;
+}
+
+// four pixels per thread; 16-bit planes whose rows start on 8 bytes move as 4-sample vectors
+__global__ void k_color(ColorJob J)
+{
+  const int x0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x), y = blockIdx.y;
+  if(x0 >= J.W || y >= J.H) return;
+  const int64_t so = (int64_t)y * J.sstride + x0, dof = (int64_t)y * J.dstride + x0;
+  const bool vec = J.sbytes == 2 && x0 + 4 <= J.W &&
+                   (((uintptr_t)J.src[0] | (uintptr_t)J.src[1] | (uintptr_t)J.src[2] | (uintptr_t)J.dst[0] |
+                     (uintptr_t)J.dst[1] | (uintptr_t)J.dst[2] | ((size_t)J.sstride * 2) | ((size_t)J.dstride * 2)) & 7) == 0;
+  if(vec)
+  {
+    uint2 in[3], outv[3];
+    #pragma unroll
+    for(int k = 0; k < 3; k++) in[k] = *reinterpret_cast<const uint2*>((const uint16_t*)J.src[k] + so);
+    uint32_t o[3][2];
+    #pragma unroll
+    for(int h = 0; h < 2; h++)
+    {
+      const uint32_t a = h ? in[0].y : in[0].x, b = h ? in[1].y : in[1].x, c = h ? in[2].y : in[2].x;
+      int p0, p1, p2, q0, q1, q2;
+      color_px(J, (int)(a & 0xFFFFu), (int)(b & 0xFFFFu), (int)(c & 0xFFFFu), p0, p1, p2);
+      color_px(J, (int)(a >> 16), (int)(b >> 16), (int)(c >> 16), q0, q1, q2);
+      o[0][h] = (uint32_t)p0 | ((uint32_t)q0 << 16);
+      o[1][h] = (uint32_t)p1 | ((uint32_t)q1 << 16);
+      o[2][h] = (uint32_t)p2 | ((uint32_t)q2 << 16);
+    }
+    #pragma unroll
+    for(int k = 0; k < 3; k++) { outv[k] = make_uint2(o[k][0], o[k][1]); *reinterpret_cast<uint2*>(J.dst[k] + dof) = outv[k]; }
+    return;
+  }
+  for(int i = 0; i < 4 && x0 + i < J.W; i++)
+  {
+    const int a = ld_rw(J.src[0], J.sbytes, so + i), b = ld_rw(J.src[1], J.sbytes, so + i), c = ld_rw(J.src[2], J.sbytes, so + i);
+    int o0, o1, o2;
+    color_px(J, a, b, c, o0, o1, o2);
+    J.dst[0][dof + i] = (uint16_t)o0;
+    J.dst[1][dof + i] = (uint16_t)o1;
+    J.dst[2][dof + i] = (uint16_t)o2;
+  }
 }
 
 }  // namespace
@@ -135,8 +199,7 @@ cudaError_t launch_upsample_h(const void* src, int sbytes, int sstride, void* ds
 cudaError_t launch_range(void* plane, int sbytes, int stride, int w, int h, int maxv, int conceal, unsigned long long* count,
                          int sms, cudaStream_t st)
 {
-  const int64_t total = (int64_t)w * h;
-  int blocks = (int)std::min<int64_t>((total + 255) / 256, (int64_t)sms * 8);
+  int blocks = std::min(h, std::max(1, sms) * 8);
   if(blocks < 1) blocks = 1;
   k_range<<<blocks, 256, 0, st>>>(plane, sbytes, stride, w, h, maxv, conceal, count);
   return cudaGetLastError();
@@ -144,7 +207,7 @@ cudaError_t launch_range(void* plane, int sbytes, int stride, int w, int h, int 
 
 cudaError_t launch_color(const ColorJob& j, cudaStream_t st)
 {
-  k_color<<<dim3((j.W + 255) / 256, j.H), 256, 0, st>>>(j);
+  k_color<<<dim3((j.W + 1023) / 1024, j.H), 256, 0, st>>>(j);
   return cudaGetLastError();
 }
 

@@ -7,11 +7,16 @@
 #include <cstdarg>
 #include <cstddef>
 #include <cstdio>
+#include <condition_variable>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
+
+#include <unistd.h>
 
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -1928,6 +1933,62 @@ qmiv_status qmiv_color_convert(const qmiv_pic* src, uint16_t* dst[3], int32_t ds
   return QMIV_OK;
 }
 
+// A frame is read by a few threads at once (pread of consecutive slices into the pinned
+// buffer): one thread copying out of the page cache reaches a fraction of the host memory
+// bandwidth. The workers persist for the reader's lifetime and wait for a generation number.
+struct YuvPool {
+  std::vector<std::thread> workers;
+  std::mutex m;
+  std::condition_variable cv, done_cv;
+  int fd = -1;
+  uint8_t* dst = nullptr;
+  int64_t off = 0, bytes = 0;
+  uint64_t gen = 0;
+  int pending = 0;
+  bool stop = false, failed = false;
+
+  void run(int id, int n)
+  {
+    uint64_t seen = 0;
+    for(;;)
+    {
+      uint8_t* d; int64_t o, b;
+      {
+        std::unique_lock<std::mutex> lk(m);
+        cv.wait(lk, [&] { return stop || gen != seen; });
+        if(stop) return;
+        seen = gen; d = dst; o = off; b = bytes;
+      }
+      // slice id of n, 4 KiB aligned
+      const int64_t per = ((b + n - 1) / n + 4095) & ~(int64_t)4095;
+      const int64_t s0 = std::min(b, per * id), s1 = std::min(b, s0 + per);
+      bool ok = true;
+      for(int64_t p = s0; p < s1 && ok;)
+      {
+        const ssize_t got = ::pread(fd, d + p, (size_t)(s1 - p), (off_t)(o + p));
+        if(got <= 0) ok = false; else p += got;
+      }
+      std::lock_guard<std::mutex> lk(m);
+      if(!ok) failed = true;
+      if(--pending == 0) done_cv.notify_all();
+    }
+  }
+  bool read(uint8_t* d, int64_t o, int64_t b)
+  {
+    std::unique_lock<std::mutex> lk(m);
+    dst = d; off = o; bytes = b; failed = false; pending = (int)workers.size(); gen++;
+    cv.notify_all();
+    done_cv.wait(lk, [&] { return pending == 0; });
+    return !failed;
+  }
+  ~YuvPool()
+  {
+    { std::lock_guard<std::mutex> lk(m); stop = true; }
+    cv.notify_all();
+    for(auto& t : workers) t.join();
+  }
+};
+
 struct qmiv_yuv_reader {
   FILE* f = nullptr;
   int32_t w = 0, h = 0, bd = 8, cf = 420, bps = 1;
@@ -1937,11 +1998,13 @@ struct qmiv_yuv_reader {
   uint8_t* d_444[2] = { nullptr, nullptr };   // 4:2:2 chroma upsampled to 4:4:4
   cudaEvent_t ev[2] = { nullptr, nullptr };
   bool used[2] = { false, false };
+  std::unique_ptr<YuvPool> pool;              // frames of 1 MiB and more
 };
 
 qmiv_status qmiv_yuv_close(qmiv_yuv_reader* r)
 {
   if(!r) return QMIV_OK;
+  r->pool.reset();
   if(r->f) std::fclose(r->f);
   for(int i = 0; i < 2; i++)
   {
@@ -1971,6 +2034,14 @@ qmiv_status qmiv_yuv_open(qmiv_yuv_reader** out, const char* path, int32_t width
   std::fseek(r->f, 0, SEEK_END);
   const long long bytes = std::ftell(r->f);
   r->frames = bytes / r->frame_bytes;  // xSeqBase counts whole frames
+  if(r->frame_bytes >= (1 << 20))
+  {
+    const unsigned hc = std::thread::hardware_concurrency();
+    const int n = (int)std::max(1u, std::min(4u, hc ? hc : 1u));
+    r->pool.reset(new YuvPool);
+    r->pool->fd = fileno(r->f);
+    for(int i = 0; i < n; i++) r->pool->workers.emplace_back([p = r->pool.get(), i, n] { p->run(i, n); });
+  }
   for(int i = 0; i < 2; i++)
   {
     if(cudaMallocHost((void**)&r->h_buf[i], r->frame_bytes) != cudaSuccess ||
@@ -1993,8 +2064,13 @@ qmiv_status qmiv_yuv_read(qmiv_yuv_reader* r, int64_t frame, qmiv_pic* out, qmiv
   const cudaStream_t st = (cudaStream_t)stream;
   const int k = (int)(frame & 1);
   if(r->used[k]) CUDA_TRY(cudaEventSynchronize(r->ev[k]));  // the slot's previous upload has finished
-  if(std::fseek(r->f, (long)(frame * r->frame_bytes), SEEK_SET) != 0 ||
-     std::fread(r->h_buf[k], 1, (size_t)r->frame_bytes, r->f) != (size_t)r->frame_bytes)
+  if(r->pool)
+  {
+    if(!r->pool->read(r->h_buf[k], frame * r->frame_bytes, r->frame_bytes))
+      return fail(QMIV_BAD_ARG, "short read of frame %lld", (long long)frame);
+  }
+  else if(std::fseek(r->f, (long)(frame * r->frame_bytes), SEEK_SET) != 0 ||
+          std::fread(r->h_buf[k], 1, (size_t)r->frame_bytes, r->f) != (size_t)r->frame_bytes)
     return fail(QMIV_BAD_ARG, "short read of frame %lld", (long long)frame);
   CUDA_TRY(cudaMemcpyAsync(r->d_raw[k], r->h_buf[k], (size_t)r->frame_bytes, cudaMemcpyHostToDevice, st));
   const int64_t area = (int64_t)r->w * r->h;
