@@ -1256,6 +1256,15 @@ qmiv_status qmiv_calc_frame_masked(qmiv_handle* h, const qmiv_pic* pic0, const q
     j.w_search[c] = h->opt.cmp_w_search[c]; j.w_avg[c] = h->opt.cmp_w_avg[c];
     j.maxdiff[c] = h->params.maxdiff_for_bd[j.bd][c];
   }
+  {
+    uint64_t bound = 0;
+    for(int c = 0; c < 3; c++)
+    {
+      const uint64_t d = (uint64_t)((1 << j.bd) - 1) + (uint64_t)std::abs(j.maxdiff[c]);
+      bound += d * d * (uint64_t)j.w_search[c];
+    }
+    j.fits32 = bound < (uint64_t)INT32_MAX;
+  }
   j.counters = reinterpret_cast<uint32_t*>(h->mask_small);
   j.nnm = reinterpret_cast<long long*>(h->mask_small + 16);
   j.gcd = reinterpret_cast<int32_t*>(h->mask_small + 32);

@@ -23,6 +23,7 @@ struct MaskJob {
   int32_t fake_exact, sr;
   int32_t w_search[3], w_avg[3], maxdiff[3];
   int32_t gcd_given;
+  int32_t fits32;                   // the largest search cost, sum of w (2^bd - 1 + maxdiff)^2, is below 2^31 - 1
   int32_t* gcd;                     // [3] device: masked GCD_R2T (written unless given)
   long long* nnm;                   // [1] device: non-masked pixel count
   int64_t* rows;                    // [H][kMaskRowVals]

@@ -94,3 +94,24 @@ def test_masked_exact_components_and_rejections(gpu_lib, oq):
             P.calc_frame_masked(gpu_lib.make_pic(p, bd), gpu_lib.make_pic(q, bd), mask, 8, gpu_lib.M_SSIM)
         with pytest.raises(gpu_lib.QmivError):
             P.calc_frame_masked(gpu_lib.make_pic(p, bd), gpu_lib.make_pic(q, bd), np.ascontiguousarray(mask[:, :10]), 8)
+
+
+@pytest.mark.parametrize("sr,bd,w_search", [(0, 10, (4, 1, 1)), (1, 10, (4, 1, 1)), (3, 8, (4, 1, 1)),
+                                            (4, 10, (4, 1, 1)), (6, 10, (4, 1, 1)), (16, 10, (2, 1, 3)),
+                                            (2, 14, (8, 1, 1)), (5, 14, (8, 1, 1))])
+def test_masked_search_ranges_and_wide_costs(gpu_lib, oq, sr, bd, w_search):
+    """Every search-range specialisation of the tiled masked search (1-4 compiled, others at run
+    time, 16 the largest halo) and the 64-bit cost form, taken when the largest possible cost
+    (14-bit samples, luma weight 8) does not fit 31 bits; the synthetic pairs' actual costs stay
+    small, so the oracle's 32-bit costs are exact there."""
+    w, h = 112, 72
+    ref, tst = synth.pair420(w, h, bd, seed=500 + sr + bd, holes=True)
+    mask = make_mask(w, h, 500 + sr, "ellipses").astype(np.uint8)
+    p0 = oq.upsample420(synth.split420(ref, w, h), w, h)
+    p1 = oq.upsample420(synth.split420(tst, w, h), w, h)
+    want = oq.masked(p0, p1, mask, bd, mask_bd=8, search_range=sr, w_search=w_search, nthreads=8)
+    dt = np.uint8 if bd == 8 else np.uint16
+    with gpu_lib.Processor(w, h, search_range=sr, cmp_w_search=w_search) as P:
+        g = P.calc_frame_masked(gpu_lib.make_pic(_planes(ref, w, h, dt), bd), gpu_lib.make_pic(_planes(tst, w, h, dt), bd),
+                                mask, 8)
+    _check(g, want)
