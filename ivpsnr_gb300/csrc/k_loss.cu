@@ -27,6 +27,8 @@ namespace qmiv {
 namespace {
 
 constexpr int kCpsTX = 32, kCpsTY = 8;
+constexpr int kLossGgPx = 1024;               // pixels per block of the GCD-gradient reduction (4 per thread)
+constexpr int kGradTX = 32, kGradTY = 16;     // gradient gather tile (two rows per thread)
 
 struct Geo {
   const float* tst;
@@ -84,11 +86,6 @@ __global__ void k_loss_gcd_final(Geo g, const double* __restrict__ part, float u
 }
 
 // ---- corresponding-pixel search, both directions ----------------------------------------------
-__device__ __forceinline__ float werr(float d0, float d1, float d2, float w0, float w1, float w2)
-{ // ((w0 d0^2) + (w1 d1^2)) + (w2 d2^2), no contraction: the same rounding as separate tensor ops
-  return __fadd_rn(__fadd_rn(__fmul_rn(w0, __fmul_rn(d0, d0)), __fmul_rn(w1, __fmul_rn(d1, d1))), __fmul_rn(w2, __fmul_rn(d2, d2)));
-}
-
 template <int SR>
 __global__ void __launch_bounds__(kCpsTX * kCpsTY) k_loss_cps(Geo g, float w0, float w1, float w2,
                                                               const float* __restrict__ gcd, uint16_t* __restrict__ maps,
@@ -97,7 +94,7 @@ __global__ void __launch_bounds__(kCpsTX * kCpsTY) k_loss_cps(Geo g, float w0, f
 {
   constexpr int SWX = kCpsTX + 2 * SR, SWY = kCpsTY + 2 * SR;
   __shared__ float2 s_rt[3][SWY][SWX];   // (ref, tst) sample pairs: one load feeds both directions
-  __shared__ float s_red[8][6];
+  __shared__ float s_red[8][12];
   const int b = blockIdx.y;
   const int bx = blockIdx.x % ((g.W + kCpsTX - 1) / kCpsTX), by = blockIdx.x / ((g.W + kCpsTX - 1) / kCpsTX);
   const int x0 = bx * kCpsTX, y0 = by * kCpsTY;
@@ -153,7 +150,9 @@ __global__ void __launch_bounds__(kCpsTX * kCpsTY) k_loss_cps(Geo g, float w0, f
         const int cx = IN ? lx + dx : min(max(x + dx - SR, 0), g.W - 1) - x0 + SR;
         const int cy = IN ? ly + dy : min(max(y + dy - SR, 0), g.H - 1) - y0 + SR;
         // both directions in packed FP32: (ref - tg, tst - rg) per component, the negated
-        // differences (their squares are the same), then werr's products and sums lane by lane
+        // differences (their squares are the same), then the weighted error
+        // ((w0 d0^2) + (w1 d1^2)) + (w2 d2^2) lane by lane, without contraction: the same
+        // rounding as separate tensor ops
         const float2 d0 = __fadd2_rn(s_rt[0][cy][cx], ntg[0]);
         const float2 d1 = __fadd2_rn(s_rt[1][cy][cx], ntg[1]);
         const float2 d2 = __fadd2_rn(s_rt[2][cy][cx], ntg[2]);
@@ -192,21 +191,24 @@ __global__ void __launch_bounds__(kCpsTX * kCpsTY) k_loss_cps(Geo g, float w0, f
     if(interior) search(std::true_type{});
     else         search(std::false_type{});
   }
-  // per-block SSE partials: [R2T c0..2, T2R c0..2]
-  float v[6] = { e1[0] * e1[0], e1[1] * e1[1], e1[2] * e1[2], e0[0] * e0[0], e0[1] * e0[1], e0[2] * e0[2] };
+  // per-block partials: squared errors [R2T c0..2, T2R c0..2], then the errors themselves (the
+  // backward's d loss / d GCD takes 2 g_sse sum(e) per direction and component from them)
+  const float v[12] = { e1[0] * e1[0], e1[1] * e1[1], e1[2] * e1[2], e0[0] * e0[0], e0[1] * e0[1], e0[2] * e0[2],
+                        e1[0], e1[1], e1[2], e0[0], e0[1], e0[2] };
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for(int i = 0; i < 6; i++)
+  #pragma unroll
+  for(int i = 0; i < 12; i++)
   {
     const float s = warp_sum(v[i]);
     if(lane == 0) s_red[warp][i] = s;
   }
   __syncthreads();
-  if(threadIdx.x < 6)
+  if(threadIdx.x < 12)
   {
     double s = 0.0;
     for(int w = 0; w < 8; w++) s += (double)s_red[w][threadIdx.x];
-    const int d = threadIdx.x / 3, c = threadIdx.x % 3;
-    sse_part[(((int64_t)b * 2 + d) * 3 + c) * blocks_per_image + blockIdx.x] = s;
+    const int half = threadIdx.x / 6, d = (threadIdx.x % 6) / 3, c = threadIdx.x % 3;
+    sse_part[((int64_t)half * g.n * 6 + ((int64_t)b * 2 + d) * 3 + c) * blocks_per_image + blockIdx.x] = s;
   }
 }
 
@@ -231,51 +233,67 @@ struct BwdArgs {
   const uint16_t* maps;      // [2][n][H][W]: argmin index (bits 0-7), unclipped SCP (bits 8-10)
   const float* dy;           // [2][n][3][H][W]: T2R then R2T
   const double* g_sse;       // [n][2][3]
-  double* g_part;            // [n*3][blocks]
+  const double* esum;        // [n][2][3]: sums of the errors (forward)
+  double* g_part;            // [n*3][blocks]: SCP terms of d loss / d GCD
   const double* g_gcd;       // [n*3] (combine pass)
   float* g_tst;
   int blocks_per_image;
 };
 
-__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
-
-// Partial sums of d loss / d GCD_c over the pixels of one 32x8 block (FP32 within the block,
-// FP64 across blocks).
-template <int SR>
+// d loss / d GCD_c = sum over pixels of 2 g_sse(R2T) e1 - 2 g_sse(T2R) e0 (the errors move
+// with +GCD and -GCD) plus the SCP terms: -dSCP1 where SCP1 = clip(R - GCD) is not clipped,
+// +dSCP0 where SCP0 = clip(T + GCD) is not. The error terms factor into 2 g_sse sum(e), whose
+// sums the forward kept; this kernel sums the SCP terms, kLossGgPx pixels per block (four per
+// thread, vector loads when the plane size allows), FP32 within the block, FP64 across blocks.
 __global__ void __launch_bounds__(256) k_loss_gcd_grad_part(BwdArgs a)
 {
   __shared__ float s_red[8][3];
   const Geo& g = a.g;
-  constexpr int side = 2 * SR + 1;
   const int b = blockIdx.y;
-  const int tiles_x = (g.W + kCpsTX - 1) / kCpsTX;
-  const int x = (blockIdx.x % tiles_x) * kCpsTX + (threadIdx.x % kCpsTX);
-  const int y = (blockIdx.x / tiles_x) * kCpsTY + (threadIdx.x / kCpsTX);
-  const bool inside = x < g.W && y < g.H;
-  const float* T = g.tst + (int64_t)b * 3 * g.plane;
-  const float* R = g.ref + (int64_t)b * 3 * g.plane;
-  const int64_t pix = (int64_t)y * g.W + x;
+  const int64_t p0 = (int64_t)blockIdx.x * kLossGgPx + 4 * threadIdx.x;
+  const uint16_t* M1 = a.maps + (int64_t)b * g.plane;
+  const uint16_t* M0 = a.maps + ((int64_t)g.n + b) * g.plane;
+  const float* D1 = a.dy + (int64_t)b * 3 * g.plane;             // d/dSCP1 (T2R)
+  const float* D0 = a.dy + ((int64_t)g.n + b) * 3 * g.plane;     // d/dSCP0 (R2T)
   float v[3] = { 0.f, 0.f, 0.f };
-  if(inside)
+  if((g.plane & 3) == 0 && p0 + 3 < g.plane)
   {
-    const int m1 = a.maps[(int64_t)b * g.plane + pix];
-    const int m0 = a.maps[((int64_t)g.n + b) * g.plane + pix];
-    const int k1 = m1 & 255, k0 = m0 & 255;
-    const int64_t q1 = (int64_t)clampi(y + k1 / side - SR, 0, g.H - 1) * g.W + clampi(x + k1 % side - SR, 0, g.W - 1);
-    const int64_t q0 = (int64_t)clampi(y + k0 / side - SR, 0, g.H - 1) * g.W + clampi(x + k0 % side - SR, 0, g.W - 1);
+    const ushort4 m1 = *reinterpret_cast<const ushort4*>(M1 + p0);
+    const ushort4 m0 = *reinterpret_cast<const ushort4*>(M0 + p0);
+    float4 d1[3], d0[3];
     #pragma unroll
     for(int c = 0; c < 3; c++)
     {
-      const float gc = a.gcd[b * 3 + c];
-      const float e1 = __fsub_rn(__fadd_rn(T[(int64_t)c * g.plane + pix], gc), R[(int64_t)c * g.plane + q1]);
-      const float e0 = __fsub_rn(__fsub_rn(R[(int64_t)c * g.plane + pix], gc), T[(int64_t)c * g.plane + q0]);
-      const float gs1 = (float)a.g_sse[(b * 2 + 0) * 3 + c], gs0 = (float)a.g_sse[(b * 2 + 1) * 3 + c];
-      float t = 2.0f * (gs1 * e1 - gs0 * e0);
-      if(m1 & (256 << c)) t -= a.dy[((int64_t)b * 3 + c) * g.plane + pix];            // T2R: d/dSCP1
-      if(m0 & (256 << c)) t += a.dy[(((int64_t)g.n + b) * 3 + c) * g.plane + pix];    // R2T: d/dSCP0
+      d1[c] = *reinterpret_cast<const float4*>(D1 + (int64_t)c * g.plane + p0);
+      d0[c] = *reinterpret_cast<const float4*>(D0 + (int64_t)c * g.plane + p0);
+    }
+    #pragma unroll
+    for(int c = 0; c < 3; c++)
+    {
+      const int bit = 256 << c;
+      float t = 0.f;
+      if(m1.x & bit) t -= d1[c].x;
+      if(m0.x & bit) t += d0[c].x;
+      if(m1.y & bit) t -= d1[c].y;
+      if(m0.y & bit) t += d0[c].y;
+      if(m1.z & bit) t -= d1[c].z;
+      if(m0.z & bit) t += d0[c].z;
+      if(m1.w & bit) t -= d1[c].w;
+      if(m0.w & bit) t += d0[c].w;
       v[c] = t;
     }
   }
+  else
+    for(int64_t p = p0; p < min(p0 + 4, g.plane); p++)
+    {
+      const int m1 = M1[p], m0 = M0[p];
+      #pragma unroll
+      for(int c = 0; c < 3; c++)
+      {
+        if(m1 & (256 << c)) v[c] -= D1[(int64_t)c * g.plane + p];
+        if(m0 & (256 << c)) v[c] += D0[(int64_t)c * g.plane + p];
+      }
+    }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   #pragma unroll
   for(int c = 0; c < 3; c++)
@@ -293,91 +311,112 @@ __global__ void __launch_bounds__(256) k_loss_gcd_grad_part(BwdArgs a)
 }
 
 // d loss / d T(q): the SSIM T2R term already in g_tst, plus the R2T error at q, plus every T2R
-// error and R2T SCP sample read from q (gathered over the window), plus the GCD term.
+// error and R2T SCP sample read from q (gathered over the window), plus the GCD term. A block
+// stages a 32x16 tile plus the search-range halo of the T2R argmin indices, the reference and
+// d/dSCP0 in shared memory, so the R2T target and every gathered neighbour are shared-memory
+// reads; each thread takes two pixels (rows ly and ly + 8).
 template <int SR>
 __global__ void __launch_bounds__(256) k_loss_grad(BwdArgs a)
 {
-  constexpr int HW = kCpsTX + 2 * kLossMaxSR, HH = kCpsTY + 2 * kLossMaxSR;
-  __shared__ uint16_t s_m0[HH][HW];
-  __shared__ float s_f[4][3];   // 2 g_sse(R2T), -2 g_sse(T2R), -g_gcd/area (or 0 when clipped)
+  constexpr int side = 2 * SR + 1;
+  constexpr int HW = kGradTX + 2 * SR, HH = kGradTY + 2 * SR, HN = HW * HH;
+  __shared__ uint16_t s_m0[HN];
+  __shared__ float s_r[3][HN];
+  __shared__ float s_d[3][HN];
+  __shared__ float s_f[4][3];   // 2 g_sse(R2T), -2 g_sse(T2R), -g_gcd/area (or 0 when clipped), GCD
   const Geo& g = a.g;
-  constexpr int side = 2 * SR + 1, sr = SR;
   const int b = blockIdx.y;
-  const int tiles_x = (g.W + kCpsTX - 1) / kCpsTX;
-  const int x0 = (blockIdx.x % tiles_x) * kCpsTX, y0 = (blockIdx.x / tiles_x) * kCpsTY;
+  const int tiles_x = (g.W + kGradTX - 1) / kGradTX;
+  const int x0 = (blockIdx.x % tiles_x) * kGradTX, y0 = (blockIdx.x / tiles_x) * kGradTY;
   const uint16_t* m0map = a.maps + ((int64_t)g.n + b) * g.plane;
-  for(int i = threadIdx.x; i < HH * HW; i += blockDim.x)
+  const float* R = g.ref + (int64_t)b * 3 * g.plane;
+  const float* D0 = a.dy + ((int64_t)g.n + b) * 3 * g.plane;
+  for(int i = threadIdx.x; i < HN; i += blockDim.x)
   {
-    const int r = i / HW, q = i % HW;
-    const int px = x0 - kLossMaxSR + q, py = y0 - kLossMaxSR + r;
+    const int r = i / HW, q = i - r * HW;
+    const int px = x0 - SR + q, py = y0 - SR + r;
+    const bool in = px >= 0 && px < g.W && py >= 0 && py < g.H;
+    const int64_t o = (int64_t)py * g.W + px;
     // outside the picture: an index that never maps back into the tile
-    s_m0[r][q] = (px >= 0 && px < g.W && py >= 0 && py < g.H) ? m0map[(int64_t)py * g.W + px] : (uint16_t)0xffffu;
+    s_m0[i] = in ? m0map[o] : (uint16_t)0xffffu;
+    #pragma unroll
+    for(int c = 0; c < 3; c++)
+    {
+      s_r[c][i] = in ? R[(int64_t)c * g.plane + o] : 0.f;
+      s_d[c][i] = in ? D0[(int64_t)c * g.plane + o] : 0.f;
+    }
   }
   if(threadIdx.x < 3)
   {
     const int c = threadIdx.x;
-    s_f[0][c] = (float)(2.0 * a.g_sse[(b * 2 + 0) * 3 + c]);
-    s_f[1][c] = (float)(-2.0 * a.g_sse[(b * 2 + 1) * 3 + c]);
-    s_f[2][c] = a.gcd_ok[b * 3 + c] ? (float)(-a.g_gcd[b * 3 + c] / (double)g.plane) : 0.0f;
+    const double gs1 = a.g_sse[(b * 2 + 0) * 3 + c], gs0 = a.g_sse[(b * 2 + 1) * 3 + c];
+    const double gg = a.g_gcd[b * 3 + c] + 2.0 * gs1 * a.esum[(b * 2 + 0) * 3 + c] - 2.0 * gs0 * a.esum[(b * 2 + 1) * 3 + c];
+    s_f[0][c] = (float)(2.0 * gs1);
+    s_f[1][c] = (float)(-2.0 * gs0);
+    s_f[2][c] = a.gcd_ok[b * 3 + c] ? (float)(-gg / (double)g.plane) : 0.0f;
     s_f[3][c] = a.gcd[b * 3 + c];
   }
   __syncthreads();
-  const int lx = threadIdx.x % kCpsTX, ly = threadIdx.x / kCpsTX;
-  const int x = x0 + lx, y = y0 + ly;
-  if(x >= g.W || y >= g.H) return;
   const float* T = g.tst + (int64_t)b * 3 * g.plane;
-  const float* R = g.ref + (int64_t)b * 3 * g.plane;
-  const int64_t q = (int64_t)y * g.W + x;
-  const int k1 = a.maps[(int64_t)b * g.plane + q] & 255;
-  const int64_t q1 = (int64_t)clampi(y + k1 / side - sr, 0, g.H - 1) * g.W + clampi(x + k1 % side - sr, 0, g.W - 1);
-  float acc[3], tq[3];
-  #pragma unroll
-  for(int c = 0; c < 3; c++)
+  const int lx = threadIdx.x % kGradTX;
+  #pragma unroll 1
+  for(int rr = 0; rr < 2; rr++)
   {
-    tq[c] = T[(int64_t)c * g.plane + q];
-    const float e1 = __fsub_rn(__fadd_rn(tq[c], s_f[3][c]), R[(int64_t)c * g.plane + q1]);
-    acc[c] = a.g_tst[((int64_t)b * 3 + c) * g.plane + q] + s_f[0][c] * e1 + s_f[2][c];
-  }
-  // pixels p = q + (dx, dy) whose T2R argmin reads q: those whose stored (clamped) displacement
-  // is (-dx, -dy); the halo's 0xffff never matches. The matches are gathered into a bit mask
-  // first and then visited in the same (row-major) order, so that a warp runs the loads of a
-  // neighbour only as many times as its busiest lane has matches, not once per neighbour.
-  constexpr int NW = (side * side + 31) / 32;
-  uint32_t hits[NW];
-  #pragma unroll
-  for(int w = 0; w < NW; w++) hits[w] = 0u;
-  #pragma unroll
-  for(int dy = -sr; dy <= sr; dy++)
+    const int ly = threadIdx.x / kGradTX + 8 * rr;
+    const int x = x0 + lx, y = y0 + ly;
+    if(x >= g.W || y >= g.H) break;
+    const int64_t q = (int64_t)y * g.W + x;
+    const int cq = (ly + SR) * HW + lx + SR;
+    // the stored index is the clamped displacement's window position: the target is inside the
+    // picture and within the halo
+    const int k1 = a.maps[(int64_t)b * g.plane + q] & 255;
+    const int c1 = cq + (k1 / side - SR) * HW + (k1 % side - SR);
+    float acc[3], tq[3];
     #pragma unroll
-    for(int dx = -sr; dx <= sr; dx++)
-      if((s_m0[ly + kLossMaxSR + dy][lx + kLossMaxSR + dx] & 255) == (sr - dy) * side + (sr - dx))
-      {
-        const int i = (dy + sr) * side + dx + sr;
-        hits[i >> 5] |= 1u << (i & 31);
-      }
-  #pragma unroll
-  for(int w = 0; w < NW; w++)
-  while(hits[w])
-  {
-    const int i = 32 * w + __ffs(hits[w]) - 1;
-    hits[w] &= hits[w] - 1;
+    for(int c = 0; c < 3; c++)
     {
-      const int dy = i / side - sr, dx = i - (i / side) * side - sr;
-      const int m0 = s_m0[ly + kLossMaxSR + dy][lx + kLossMaxSR + dx];
-      const int px = x + dx, py = y + dy;
-      const int64_t p = (int64_t)py * g.W + px;
-      #pragma unroll
-      for(int c = 0; c < 3; c++)
-      {
-        const float e0 = __fsub_rn(__fsub_rn(R[(int64_t)c * g.plane + p], s_f[3][c]), tq[c]);
-        float v = s_f[1][c] * e0;
-        if(m0 & (256 << c)) v += a.dy[(((int64_t)g.n + b) * 3 + c) * g.plane + p];
-        acc[c] += v;
-      }
+      tq[c] = T[(int64_t)c * g.plane + q];
+      const float e1 = __fsub_rn(__fadd_rn(tq[c], s_f[3][c]), s_r[c][c1]);
+      acc[c] = a.g_tst[((int64_t)b * 3 + c) * g.plane + q] + s_f[0][c] * e1 + s_f[2][c];
     }
+    // pixels p = q + (dx, dy) whose T2R argmin reads q: those whose stored (clamped) displacement
+    // is (-dx, -dy); the halo's 0xffff never matches. The matches are gathered into a bit mask
+    // first and then visited in the same (row-major) order, so that a warp runs the reads of a
+    // neighbour only as many times as its busiest lane has matches, not once per neighbour.
+    constexpr int NW = (side * side + 31) / 32;
+    uint32_t hits[NW];
+    #pragma unroll
+    for(int w = 0; w < NW; w++) hits[w] = 0u;
+    #pragma unroll
+    for(int dy = -SR; dy <= SR; dy++)
+      #pragma unroll
+      for(int dx = -SR; dx <= SR; dx++)
+        if((s_m0[cq + dy * HW + dx] & 255) == (SR - dy) * side + (SR - dx))
+        {
+          const int i = (dy + SR) * side + dx + SR;
+          hits[i >> 5] |= 1u << (i & 31);
+        }
+    #pragma unroll
+    for(int w = 0; w < NW; w++)
+      while(hits[w])
+      {
+        const int i = 32 * w + __ffs(hits[w]) - 1;
+        hits[w] &= hits[w] - 1;
+        const int dy = i / side - SR, dx = i - (i / side) * side - SR;
+        const int pi = cq + dy * HW + dx;
+        const int m0 = s_m0[pi];
+        #pragma unroll
+        for(int c = 0; c < 3; c++)
+        {
+          const float e0 = __fsub_rn(__fsub_rn(s_r[c][pi], s_f[3][c]), tq[c]);
+          float v = s_f[1][c] * e0;
+          if(m0 & (256 << c)) v += s_d[c][pi];
+          acc[c] += v;
+        }
+      }
+    #pragma unroll
+    for(int c = 0; c < 3; c++) a.g_tst[((int64_t)b * 3 + c) * g.plane + q] = acc[c];
   }
-  #pragma unroll
-  for(int c = 0; c < 3; c++) a.g_tst[((int64_t)b * 3 + c) * g.plane + q] = acc[c];
 }
 
 size_t al256(size_t v) { return (v + 255) & ~(size_t)255; }
@@ -392,17 +431,20 @@ LossLayout loss_layout(int n, int W, int H, int window)
   L.tiles_x = ssim_tiles_x(W, window);
   L.tiles_y = ssim_tiles_y(H);
   L.cps_blocks = ((W + kCpsTX - 1) / kCpsTX) * ((H + kCpsTY - 1) / kCpsTY);
+  L.gg_blocks = (int)(((int64_t)W * H + kLossGgPx - 1) / kLossGgPx);
+  L.grad_blocks = ((W + kGradTX - 1) / kGradTX) * ((H + kGradTY - 1) / kGradTY);
   const size_t plane = (size_t)W * H;
   size_t o = 0;
   L.gcd_part = o; o += al256(sizeof(double) * n * 3 * kLossGcdChunks);
   L.gcd = o;      o += al256(sizeof(float) * n * 3) + al256(sizeof(int) * n * 3);
   L.maps = o;     o += al256(sizeof(uint16_t) * 2 * (size_t)n * plane);
   L.scp = o;      o += al256(sizeof(float) * 2 * (size_t)n * 3 * plane);
-  L.sse_part = o; o += al256(sizeof(double) * (size_t)n * 6 * L.cps_blocks);
+  L.sse_part = o; o += al256(sizeof(double) * 2 * (size_t)n * 6 * L.cps_blocks);
+  L.esum = o;     o += al256(sizeof(double) * (size_t)n * 6);
   L.sjobs = o;    o += al256(std::max(sizeof(SsimJob), sizeof(SsimBwdJob)) * n * 6);
   L.partial = o;  o += al256(sizeof(float) * (size_t)n * 6 * std::max(0, H - 10) * L.tiles_x);
   L.dy = o;       o += al256(sizeof(float) * 2 * (size_t)n * 3 * plane);
-  L.g_part = o;   o += al256(sizeof(double) * (size_t)n * 3 * L.cps_blocks) + al256(sizeof(double) * n * 3);
+  L.g_part = o;   o += al256(sizeof(double) * (size_t)n * 3 * L.gg_blocks) + al256(sizeof(double) * n * 3);
   L.bytes = o;
   return L;
 }
@@ -428,6 +470,8 @@ cudaError_t loss_forward(const LossArgs& a, double* sse, double* ssim, cudaStrea
     default: k_loss_cps<4><<<grid, kCpsTX * kCpsTY, 0, st>>>(g, a.w_search[0], a.w_search[1], a.w_search[2], gcd, maps, scp, ssep, L.cps_blocks); break;
   }
   k_loss_sum_parts<<<a.n * 6, 32, 0, st>>>(ssep, L.cps_blocks, a.n * 6, sse, 1.0);
+  k_loss_sum_parts<<<a.n * 6, 32, 0, st>>>(ssep + (size_t)a.n * 6 * L.cps_blocks, L.cps_blocks, a.n * 6,
+                                           (double*)(a.ws + L.esum), 1.0);
   // SSIM jobs: (b, d, c) -> ssim[b][d][c]; d 0 = R2T: SSIM(R, SCP0), d 1 = T2R: SSIM(T, SCP1)
   std::vector<SsimJob> jobs(a.n * 6);
   const size_t plane = (size_t)a.W * a.H;
@@ -497,26 +541,21 @@ cudaError_t loss_backward(const LossArgs& a, const double* g_sse, const double* 
   ba.maps = (const uint16_t*)(a.ws + L.maps);
   ba.dy = dy;
   ba.g_sse = g_sse;
+  ba.esum = (const double*)(a.ws + L.esum);
   ba.g_part = (double*)(a.ws + L.g_part);
-  double* g_gcd = (double*)(a.ws + L.g_part + al256(sizeof(double) * (size_t)a.n * 3 * L.cps_blocks));
+  double* g_gcd = (double*)(a.ws + L.g_part + al256(sizeof(double) * (size_t)a.n * 3 * L.gg_blocks));
   ba.g_gcd = g_gcd;
   ba.g_tst = g_tst;
-  ba.blocks_per_image = L.cps_blocks;
-  const dim3 grid(L.cps_blocks, a.n);
+  ba.blocks_per_image = L.gg_blocks;
+  k_loss_gcd_grad_part<<<dim3(L.gg_blocks, a.n), 256, 0, st>>>(ba);
+  k_loss_sum_parts<<<a.n * 3, 32, 0, st>>>(ba.g_part, L.gg_blocks, a.n * 3, g_gcd, 1.0);
+  const dim3 grid(L.grad_blocks, a.n);
   switch(a.sr)
   {
-    case 1: k_loss_gcd_grad_part<1><<<grid, kCpsTX * kCpsTY, 0, st>>>(ba); break;
-    case 2: k_loss_gcd_grad_part<2><<<grid, kCpsTX * kCpsTY, 0, st>>>(ba); break;
-    case 3: k_loss_gcd_grad_part<3><<<grid, kCpsTX * kCpsTY, 0, st>>>(ba); break;
-    default: k_loss_gcd_grad_part<4><<<grid, kCpsTX * kCpsTY, 0, st>>>(ba); break;
-  }
-  k_loss_sum_parts<<<a.n * 3, 32, 0, st>>>(ba.g_part, L.cps_blocks, a.n * 3, g_gcd, 1.0);
-  switch(a.sr)
-  {
-    case 1: k_loss_grad<1><<<grid, kCpsTX * kCpsTY, 0, st>>>(ba); break;
-    case 2: k_loss_grad<2><<<grid, kCpsTX * kCpsTY, 0, st>>>(ba); break;
-    case 3: k_loss_grad<3><<<grid, kCpsTX * kCpsTY, 0, st>>>(ba); break;
-    default: k_loss_grad<4><<<grid, kCpsTX * kCpsTY, 0, st>>>(ba); break;
+    case 1: k_loss_grad<1><<<grid, 256, 0, st>>>(ba); break;
+    case 2: k_loss_grad<2><<<grid, 256, 0, st>>>(ba); break;
+    case 3: k_loss_grad<3><<<grid, 256, 0, st>>>(ba); break;
+    default: k_loss_grad<4><<<grid, 256, 0, st>>>(ba); break;
   }
   return cudaGetLastError();
 }

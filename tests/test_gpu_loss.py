@@ -14,10 +14,10 @@ def _pair(n, w, h, seed):
     import torch
     from ivpsnr_gb300 import synth
     rs, ts = [], []
-    for i in range(n):
-        r, t = synth.float444(w, h, seed=seed + i)
-        rs.append(r)
-        ts.append(t)
+    for i in range(n):  # the generator takes even sizes: odd ones are cropped from the next even size
+        r, t = synth.float444(w + w % 2, h + h % 2, seed=seed + i)
+        rs.append(np.ascontiguousarray(r[:, :h, :w]))
+        ts.append(np.ascontiguousarray(t[:, :h, :w]))
     return torch.from_numpy(np.stack(ts)), torch.from_numpy(np.stack(rs))
 
 
@@ -49,7 +49,10 @@ def _ref(tst, ref, a, b, dtype, **kw):
 
 
 CASES = [(2, 160, 128, 11, {}), (1, 96, 80, 12, {"search_range": 1}), (1, 128, 64, 13, {"ssim_window": 1}),
-         (1, 64, 48, 14, {"search_range": 3, "unnoticeable": (0.001, 0.03, 0.03)})]
+         (1, 64, 48, 14, {"search_range": 3, "unnoticeable": (0.001, 0.03, 0.03)}),
+         # ragged tiles: 100x70 (partial 32x16 tiles, plane a multiple of 4) at the largest range,
+         # 99x37 (plane not a multiple of 4: the scalar reduction path)
+         (1, 100, 70, 15, {"search_range": 4}), (2, 99, 37, 16, {})]
 
 
 def _kw(opts):
