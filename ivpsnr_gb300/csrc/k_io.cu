@@ -33,9 +33,9 @@ __global__ void k_upsample_h(const void* __restrict__ src, int sbytes, int sstri
   else            ((uint16_t*)dst)[(int64_t)y * W + x] = (uint16_t)v;
 }
 
-// count samples above Max in one plane; optionally clip them in place. A block walks rows
-// (grid-stride over rows, threads over columns), 16-bit rows in 8-sample vectors when the row
-// starts on 16 bytes, so no 64-bit division per sample.
+// count samples above Max per plane; optionally clip them in place. grid.y is the component; a
+// block walks rows (grid-stride over rows, threads over columns), 16-bit rows in 8-sample vectors
+// when the row starts on 16 bytes, so no 64-bit division per sample.
 __device__ __forceinline__ unsigned range_word(uint32_t& w, int maxv, int conceal)
 { // two 16-bit samples
   const int lo = (int)(w & 0xFFFFu), hi = (int)(w >> 16);
@@ -44,10 +44,17 @@ __device__ __forceinline__ unsigned range_word(uint32_t& w, int maxv, int concea
   return n;
 }
 
-__global__ void __launch_bounds__(256) k_range(void* plane, int sbytes, int stride, int w, int h, int maxv, int conceal,
-                                               unsigned long long* count)
+__global__ void __launch_bounds__(256) k_range(RangeJob J)
 {
   __shared__ unsigned int s_n[8];
+  const int c = blockIdx.y;
+  // fields of component c by selection: a runtime index into the parameter arrays would copy
+  // them to local memory
+  void* const plane = c == 0 ? J.plane[0] : (c == 1 ? J.plane[1] : J.plane[2]);
+  const int stride = c == 0 ? J.stride[0] : (c == 1 ? J.stride[1] : J.stride[2]);
+  const int w = c == 0 ? J.w[0] : (c == 1 ? J.w[1] : J.w[2]);
+  const int h = c == 0 ? J.h[0] : (c == 1 ? J.h[1] : J.h[2]);
+  const int maxv = J.maxv, conceal = J.conceal, sbytes = J.sbytes;
   unsigned int n = 0;
   const bool vec = sbytes == 2 && ((((uintptr_t)plane) | ((size_t)stride * 2)) & 15) == 0;
   for(int y = blockIdx.x; y < h; y += gridDim.x)
@@ -56,13 +63,25 @@ __global__ void __launch_bounds__(256) k_range(void* plane, int sbytes, int stri
     {
       uint4* row = reinterpret_cast<uint4*>((uint16_t*)plane + (int64_t)y * stride);
       const int nv = w >> 3;
-      for(int i = threadIdx.x; i < nv; i += blockDim.x)
-      {
-        uint4 v = row[i];
-        const unsigned c = range_word(v.x, maxv, conceal) + range_word(v.y, maxv, conceal) +
-                           range_word(v.z, maxv, conceal) + range_word(v.w, maxv, conceal);
-        n += c;
-        if(conceal && c) row[i] = v;
+      for(int i0 = threadIdx.x; i0 < nv; i0 += 4 * blockDim.x)
+      { // four independent 16-byte loads in flight per thread
+        uint4 v[4];
+        #pragma unroll
+        for(int k = 0; k < 4; k++)
+        {
+          const int i = i0 + k * blockDim.x;
+          if(i < nv) v[k] = row[i];
+        }
+        #pragma unroll
+        for(int k = 0; k < 4; k++)
+        {
+          const int i = i0 + k * blockDim.x;
+          if(i >= nv) break;
+          const unsigned m = range_word(v[k].x, maxv, conceal) + range_word(v[k].y, maxv, conceal) +
+                             range_word(v[k].z, maxv, conceal) + range_word(v[k].w, maxv, conceal);
+          n += m;
+          if(conceal && m) row[i] = v[k];
+        }
       }
       for(int x = 8 * nv + threadIdx.x; x < w; x += blockDim.x)
       {
@@ -93,7 +112,7 @@ __global__ void __launch_bounds__(256) k_range(void* plane, int sbytes, int stri
   {
     unsigned int t = 0;
     for(int k = 0; k < 8; k++) t += s_n[k];
-    if(t) atomicAdd(count, (unsigned long long)t);
+    if(t) atomicAdd(J.count + c, (unsigned long long)t);
   }
 }
 
@@ -196,12 +215,12 @@ cudaError_t launch_upsample_h(const void* src, int sbytes, int sstride, void* ds
   return cudaGetLastError();
 }
 
-cudaError_t launch_range(void* plane, int sbytes, int stride, int w, int h, int maxv, int conceal, unsigned long long* count,
-                         int sms, cudaStream_t st)
+cudaError_t launch_range(const RangeJob& j, int sms, cudaStream_t st)
 {
-  int blocks = std::min(h, std::max(1, sms) * 8);
-  if(blocks < 1) blocks = 1;
-  k_range<<<blocks, 256, 0, st>>>(plane, sbytes, stride, w, h, maxv, conceal, count);
+  const int hmax = std::max(j.h[0], std::max(j.h[1], j.h[2]));
+  // about 8 blocks per SM over the three planes together
+  const int blocks = std::max(1, std::min(hmax, (std::max(1, sms) * 8 + 2) / 3));
+  k_range<<<dim3(blocks, 3), 256, 0, st>>>(j);
   return cudaGetLastError();
 }
 

@@ -212,16 +212,19 @@ __global__ void __launch_bounds__(kCpsTX * kCpsTY) k_loss_cps(Geo g, float w0, f
   }
 }
 
-// sum of per-block partials: out[i] = sum_k part[i][k] (fixed order), one warp per output
-__global__ void k_loss_sum_parts(const double* __restrict__ part, int nparts, int nout, double* __restrict__ out,
-                                 double scale)
+// sum of per-block partials: out[i] = sum_k part[i][k] (compensated, fixed order), one
+// 256-thread block per output: FP64 adds are slow on this part, so they are spread wide
+constexpr int kSumThreads = 256;
+__global__ void __launch_bounds__(kSumThreads) k_loss_sum_parts(const double* __restrict__ part, int nparts, int nout,
+                                                                double* __restrict__ out, double scale)
 {
+  __shared__ double scratch[2 * (kSumThreads / 32)];
   const int i = blockIdx.x;
   if(i >= nout) return;
   Kbns k = { 0.0, 0.0 };
-  for(int j = threadIdx.x; j < nparts; j += 32) k = kbns_add(k, part[(int64_t)i * nparts + j]);
-  k = warp_kbns(k);
-  if(threadIdx.x == 0) out[i] = kbns_result(k) * scale;
+  for(int j = threadIdx.x; j < nparts; j += kSumThreads) k = kbns_add(k, part[(int64_t)i * nparts + j]);
+  const double t = block_kbns(k, scratch);
+  if(threadIdx.x == 0) out[i] = t * scale;
 }
 
 // ---- backward -------------------------------------------------------------------------------
@@ -469,8 +472,8 @@ cudaError_t loss_forward(const LossArgs& a, double* sse, double* ssim, cudaStrea
     case 3: k_loss_cps<3><<<grid, kCpsTX * kCpsTY, 0, st>>>(g, a.w_search[0], a.w_search[1], a.w_search[2], gcd, maps, scp, ssep, L.cps_blocks); break;
     default: k_loss_cps<4><<<grid, kCpsTX * kCpsTY, 0, st>>>(g, a.w_search[0], a.w_search[1], a.w_search[2], gcd, maps, scp, ssep, L.cps_blocks); break;
   }
-  k_loss_sum_parts<<<a.n * 6, 32, 0, st>>>(ssep, L.cps_blocks, a.n * 6, sse, 1.0);
-  k_loss_sum_parts<<<a.n * 6, 32, 0, st>>>(ssep + (size_t)a.n * 6 * L.cps_blocks, L.cps_blocks, a.n * 6,
+  k_loss_sum_parts<<<a.n * 6, kSumThreads, 0, st>>>(ssep, L.cps_blocks, a.n * 6, sse, 1.0);
+  k_loss_sum_parts<<<a.n * 6, kSumThreads, 0, st>>>(ssep + (size_t)a.n * 6 * L.cps_blocks, L.cps_blocks, a.n * 6,
                                            (double*)(a.ws + L.esum), 1.0);
   // SSIM jobs: (b, d, c) -> ssim[b][d][c]; d 0 = R2T: SSIM(R, SCP0), d 1 = T2R: SSIM(T, SCP1)
   std::vector<SsimJob> jobs(a.n * 6);
@@ -548,7 +551,7 @@ cudaError_t loss_backward(const LossArgs& a, const double* g_sse, const double* 
   ba.g_tst = g_tst;
   ba.blocks_per_image = L.gg_blocks;
   k_loss_gcd_grad_part<<<dim3(L.gg_blocks, a.n), 256, 0, st>>>(ba);
-  k_loss_sum_parts<<<a.n * 3, 32, 0, st>>>(ba.g_part, L.gg_blocks, a.n * 3, g_gcd, 1.0);
+  k_loss_sum_parts<<<a.n * 3, kSumThreads, 0, st>>>(ba.g_part, L.gg_blocks, a.n * 3, g_gcd, 1.0);
   const dim3 grid(L.grad_blocks, a.n);
   switch(a.sr)
   {

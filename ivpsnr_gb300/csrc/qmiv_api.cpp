@@ -1897,26 +1897,54 @@ static qmiv_status check_device_pic(const qmiv_pic* p, const char* name)
   return QMIV_OK;
 }
 
+// Counters of qmiv_check_range: per calling thread and device, 3 device counters and their
+// pinned host copy, made on the first call and kept (a call is synchronous, so a thread's
+// calls never overlap; other threads have their own).
+struct RangeCounters {
+  unsigned long long* d[kStaticMaxDevices] = {};
+  unsigned long long* h[kStaticMaxDevices] = {};
+  ~RangeCounters()
+  {
+    for(int i = 0; i < kStaticMaxDevices; i++)
+    {
+      if(d[i]) cudaFree(d[i]);
+      if(h[i]) cudaFreeHost(h[i]);
+    }
+  }
+};
+
 qmiv_status qmiv_check_range(const qmiv_pic* pic, int32_t conceal, int64_t out_of_range[3], qmiv_stream stream)
 {
   qmiv_status s = check_device_pic(pic, "pic");
   if(s != QMIV_OK) return s;
   if(!out_of_range) return fail(QMIV_BAD_ARG, "out_of_range is null");
   const cudaStream_t st = (cudaStream_t)stream;
-  unsigned long long* d_cnt = nullptr;
-  CUDA_TRY(cudaMallocAsync((void**)&d_cnt, 3 * sizeof(unsigned long long), st));
+  thread_local RangeCounters rc;
+  int slot = 0;
+  CUDA_TRY(cudaGetDevice(&slot));
+  if(slot < 0 || slot >= kStaticMaxDevices) return fail(QMIV_UNSUPPORTED, "device %d: at most %d devices", slot, kStaticMaxDevices);
+  if(!rc.d[slot])
+  {
+    CUDA_TRY(cudaMalloc((void**)&rc.d[slot], 3 * sizeof(unsigned long long)));
+    CUDA_TRY(cudaHostAlloc((void**)&rc.h[slot], 3 * sizeof(unsigned long long), cudaHostAllocDefault));
+  }
+  unsigned long long* d_cnt = rc.d[slot];
   CUDA_TRY(cudaMemsetAsync(d_cnt, 0, 3 * sizeof(unsigned long long), st));
   const int maxv = pic->bitdepth >= 16 ? 65535 : (1 << pic->bitdepth) - 1;
-  const int sms = device_sms();
+  RangeJob j;
+  std::memset(&j, 0, sizeof(j));
   for(int c = 0; c < 3; c++)
   {
     const bool sub = c && pic->chroma_format == QMIV_CF420;
-    CUDA_TRY(launch_range(const_cast<void*>(pic->plane[c]), pic->sample_bytes, pic->stride[c], sub ? pic->width / 2 : pic->width,
-                          sub ? pic->height / 2 : pic->height, maxv, conceal ? 1 : 0, d_cnt + c, sms, st));
+    j.plane[c] = const_cast<void*>(pic->plane[c]);
+    j.stride[c] = pic->stride[c];
+    j.w[c] = sub ? pic->width / 2 : pic->width;
+    j.h[c] = sub ? pic->height / 2 : pic->height;
   }
-  unsigned long long h[3];
-  CUDA_TRY(cudaMemcpyAsync(h, d_cnt, sizeof(h), cudaMemcpyDeviceToHost, st));
-  CUDA_TRY(cudaFreeAsync(d_cnt, st));
+  j.sbytes = pic->sample_bytes; j.maxv = maxv; j.conceal = conceal ? 1 : 0; j.count = d_cnt;
+  CUDA_TRY(launch_range(j, device_sms(), st));
+  unsigned long long* h = rc.h[slot];
+  CUDA_TRY(cudaMemcpyAsync(h, d_cnt, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaStreamSynchronize(st));
   for(int c = 0; c < 3; c++) out_of_range[c] = (int64_t)h[c];
   return QMIV_OK;

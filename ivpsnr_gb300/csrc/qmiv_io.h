@@ -25,8 +25,14 @@ struct ColorJob {
 void color_matrix(int space, bool to_ycbcr, int32_t m[3][3]);
 
 cudaError_t launch_upsample_h(const void* src, int sbytes, int sstride, void* dst, int W, int H, cudaStream_t st);
-cudaError_t launch_range(void* plane, int sbytes, int stride, int w, int h, int maxv, int conceal, unsigned long long* count,
-                         int sms, cudaStream_t st);
+// The three planes of one range check / concealment (one launch, grid.y = component).
+struct RangeJob {
+  void* plane[3];
+  int32_t stride[3], w[3], h[3];
+  int32_t sbytes, maxv, conceal;
+  unsigned long long* count;  // [3] device counters
+};
+cudaError_t launch_range(const RangeJob& j, int sms, cudaStream_t st);
 cudaError_t launch_color(const ColorJob& j, cudaStream_t st);
 
 }  // namespace qmiv
