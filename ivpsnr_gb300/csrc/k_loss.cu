@@ -424,6 +424,64 @@ __global__ void __launch_bounds__(256) k_loss_grad(BwdArgs a)
 
 size_t al256(size_t v) { return (v + 255) & ~(size_t)255; }
 
+// The SSIM jobs of the loss, job k = (b * 2 + d) * 3 + c: d 0 = R2T: SSIM(R, SCP0), d 1 = T2R:
+// SSIM(T, SCP1). One definition serves the host (tile counts) and the device: the tables are
+// written on the device from this by-value descriptor, so a call copies no host memory.
+struct LossSsimDesc {
+  const float* ref;
+  const float* tst;
+  const float* scp;
+  float* partial;        // forward: per-tile row sums
+  double* ssim;          // forward: values [n][2][3]
+  const double* g_ssim;  // backward: upstream gradients [n][2][3]
+  float* g_tst;          // backward: d/dT
+  float* dy;             // backward: d/dSCP, T2R then R2T
+  int n, W, H, tiles_x, tiles_y, btx, bty;
+};
+
+__host__ __device__ inline SsimJob loss_ssim_job(const LossSsimDesc& D, int k)
+{
+  const int b = k / 6, d = (k / 3) % 2, c = k % 3;
+  const size_t plane = (size_t)D.W * D.H;
+  SsimJob j{};
+  j.a.ptr = (d == 0 ? D.ref : D.tst) + ((size_t)b * 3 + c) * plane; j.a.stride = D.W; j.a.sbytes = 4; j.a.shift = 0;
+  j.b.ptr = D.scp + (((size_t)(d == 0 ? D.n : 0) + b) * 3 + c) * plane; j.b.stride = D.W; j.b.sbytes = 4; j.b.shift = 0;
+  j.W = D.W; j.H = D.H; j.calc_l = 1;
+  j.c1 = 0.01f * 0.01f; j.c2 = 0.03f * 0.03f;
+  j.tiles_x = D.tiles_x; j.tiles_y = D.tiles_y; j.tile_base = k * D.tiles_x * D.tiles_y;
+  j.partial = D.partial + (size_t)k * (D.H > 10 ? D.H - 10 : 0) * D.tiles_x;
+  j.out = D.ssim + k;
+  return j;
+}
+
+// T2R (d 1) writes d/dT into g_tst and d/dSCP1 into dy[0]; R2T (d 0) writes d/dSCP0 into dy[1]
+__host__ __device__ inline SsimBwdJob loss_ssim_bwd_job(const LossSsimDesc& D, int k)
+{
+  const int b = k / 6, d = (k / 3) % 2, c = k % 3;
+  const size_t plane = (size_t)D.W * D.H, pl = ((size_t)b * 3 + c) * plane;
+  SsimBwdJob j{};
+  j.a.ptr = (d == 0 ? D.ref : D.tst) + pl; j.a.stride = D.W; j.a.sbytes = 4;
+  j.b.ptr = D.scp + (((size_t)(d == 0 ? D.n : 0) + b) * 3 + c) * plane; j.b.stride = D.W; j.b.sbytes = 4;
+  j.W = D.W; j.H = D.H; j.c1 = 0.01f * 0.01f; j.c2 = 0.03f * 0.03f;
+  j.tiles_x = D.btx; j.tiles_y = D.bty; j.tile_base = k * D.btx * D.bty;
+  j.g = D.g_ssim + k;
+  j.outx = d == 1 ? D.g_tst + pl : nullptr;
+  j.outy = D.dy + (((size_t)(d == 1 ? 0 : D.n) + b) * 3 + c) * plane;
+  return j;
+}
+
+__global__ void k_loss_ssim_jobs(LossSsimDesc D, SsimJob* __restrict__ out)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if(k < D.n * 6) out[k] = loss_ssim_job(D, k);
+}
+
+__global__ void k_loss_ssim_bwd_jobs(LossSsimDesc D, SsimBwdJob* __restrict__ out)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if(k < D.n * 6) out[k] = loss_ssim_bwd_job(D, k);
+}
+
 }  // namespace
 
 LossLayout loss_layout(int n, int W, int H, int window)
@@ -475,32 +533,16 @@ cudaError_t loss_forward(const LossArgs& a, double* sse, double* ssim, cudaStrea
   k_loss_sum_parts<<<a.n * 6, kSumThreads, 0, st>>>(ssep, L.cps_blocks, a.n * 6, sse, 1.0);
   k_loss_sum_parts<<<a.n * 6, kSumThreads, 0, st>>>(ssep + (size_t)a.n * 6 * L.cps_blocks, L.cps_blocks, a.n * 6,
                                            (double*)(a.ws + L.esum), 1.0);
-  // SSIM jobs: (b, d, c) -> ssim[b][d][c]; d 0 = R2T: SSIM(R, SCP0), d 1 = T2R: SSIM(T, SCP1)
-  std::vector<SsimJob> jobs(a.n * 6);
-  const size_t plane = (size_t)a.W * a.H;
-  float* part = (float*)(a.ws + L.partial);
-  int base = 0;
-  for(int b = 0; b < a.n; b++)
-    for(int d = 0; d < 2; d++)
-      for(int c = 0; c < 3; c++)
-      {
-        SsimJob& j = jobs[(b * 2 + d) * 3 + c];
-        std::memset(&j, 0, sizeof(j));
-        const float* first = (d == 0 ? a.ref : a.tst) + ((size_t)b * 3 + c) * plane;
-        const float* second = scp + (((size_t)(d == 0 ? a.n : 0) + b) * 3 + c) * plane;
-        j.a.ptr = first; j.a.stride = a.W; j.a.sbytes = 4; j.a.shift = 0;
-        j.b.ptr = second; j.b.stride = a.W; j.b.sbytes = 4; j.b.shift = 0;
-        j.W = a.W; j.H = a.H; j.calc_l = 1;
-        j.c1 = 0.01f * 0.01f; j.c2 = 0.03f * 0.03f;
-        j.tiles_x = L.tiles_x; j.tiles_y = L.tiles_y; j.tile_base = base;
-        base += L.tiles_x * L.tiles_y;
-        j.partial = part + (size_t)((b * 2 + d) * 3 + c) * std::max(0, a.H - 10) * L.tiles_x;
-        j.out = ssim + (b * 2 + d) * 3 + c;
-      }
+  // SSIM jobs: (b, d, c) -> ssim[b][d][c], their table written on the device
+  LossSsimDesc D{};
+  D.ref = a.ref; D.tst = a.tst; D.scp = scp; D.partial = (float*)(a.ws + L.partial); D.ssim = ssim;
+  D.n = a.n; D.W = a.W; D.H = a.H; D.tiles_x = L.tiles_x; D.tiles_y = L.tiles_y;
+  const int nj = a.n * 6;
+  std::vector<SsimJob> jobs(nj);
+  for(int k = 0; k < nj; k++) jobs[k] = loss_ssim_job(D, k);
   SsimJob* d_jobs = (SsimJob*)(a.ws + L.sjobs);
-  cudaError_t e = cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(SsimJob) * jobs.size(), cudaMemcpyHostToDevice, st);
-  if(e != cudaSuccess) return e;
-  e = launch_ssim(d_jobs, jobs.data(), (int)jobs.size(), a.window, st);
+  k_loss_ssim_jobs<<<(nj + 127) / 128, 128, 0, st>>>(D, d_jobs);
+  cudaError_t e = launch_ssim(d_jobs, jobs.data(), nj, a.window, st);
   if(e != cudaSuccess) return e;
   return cudaGetLastError();
 }
@@ -509,33 +551,18 @@ cudaError_t loss_backward(const LossArgs& a, const double* g_sse, const double* 
 {
   const LossLayout& L = a.L;
   Geo g = { a.tst, a.ref, a.n, a.W, a.H, (int64_t)a.W * a.H };
-  const size_t plane = (size_t)a.W * a.H;
   float* scp = (float*)(a.ws + L.scp);
   float* dy = (float*)(a.ws + L.dy);
-  // SSIM backward: T2R (d 1) writes d/dT into g_tst and d/dSCP1 into dy[0]; R2T (d 0) writes d/dSCP0 into dy[1]
-  std::vector<SsimBwdJob> jobs;
-  int base = 0;
-  const int tx = ssim_bwd_tiles(a.W), ty = ssim_bwd_tiles(a.H);
-  for(int b = 0; b < a.n; b++)
-    for(int d = 0; d < 2; d++)
-      for(int c = 0; c < 3; c++)
-      {
-        SsimBwdJob j;
-        std::memset(&j, 0, sizeof(j));
-        const size_t pl = ((size_t)b * 3 + c) * plane;
-        j.a.ptr = (d == 0 ? a.ref : a.tst) + pl; j.a.stride = a.W; j.a.sbytes = 4;
-        j.b.ptr = scp + (((size_t)(d == 0 ? a.n : 0) + b) * 3 + c) * plane; j.b.stride = a.W; j.b.sbytes = 4;
-        j.W = a.W; j.H = a.H; j.c1 = 0.01f * 0.01f; j.c2 = 0.03f * 0.03f;
-        j.tiles_x = tx; j.tiles_y = ty; j.tile_base = base; base += tx * ty;
-        j.g = g_ssim + (b * 2 + d) * 3 + c;
-        j.outx = d == 1 ? g_tst + pl : nullptr;
-        j.outy = dy + (((size_t)(d == 1 ? 0 : a.n) + b) * 3 + c) * plane;
-        jobs.push_back(j);
-      }
+  // SSIM backward jobs, their table written on the device
+  LossSsimDesc D{};
+  D.ref = a.ref; D.tst = a.tst; D.scp = scp; D.g_ssim = g_ssim; D.g_tst = g_tst; D.dy = dy;
+  D.n = a.n; D.W = a.W; D.H = a.H; D.btx = ssim_bwd_tiles(a.W); D.bty = ssim_bwd_tiles(a.H);
+  const int nj = a.n * 6;
+  std::vector<SsimBwdJob> jobs(nj);
+  for(int k = 0; k < nj; k++) jobs[k] = loss_ssim_bwd_job(D, k);
   SsimBwdJob* d_jobs = (SsimBwdJob*)(a.ws + L.sjobs);
-  cudaError_t e = cudaMemcpyAsync(d_jobs, jobs.data(), sizeof(SsimBwdJob) * jobs.size(), cudaMemcpyHostToDevice, st);
-  if(e != cudaSuccess) return e;
-  e = launch_ssim_bwd(d_jobs, jobs.data(), (int)jobs.size(), a.window, st);
+  k_loss_ssim_bwd_jobs<<<(nj + 127) / 128, 128, 0, st>>>(D, d_jobs);
+  cudaError_t e = launch_ssim_bwd(d_jobs, jobs.data(), nj, a.window, st);
   if(e != cudaSuccess) return e;
   BwdArgs ba;
   ba.g = g; ba.sr = a.sr;

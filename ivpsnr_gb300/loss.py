@@ -66,16 +66,20 @@ def iv_metrics(tst, ref, **opts):
     return IVMetricsFunction.apply(tst, ref, default_options(**opts))
 
 
+def _wmean(x, w_avg):
+    """Weighted mean over the last (component) axis with Python-scalar weights: no weight tensor
+    is made on the device, so the helpers add no host-to-device copy to a training step."""
+    w0, w1, w2 = (float(v) for v in w_avg)
+    return (x[..., 0] * w0 + x[..., 1] * w1 + x[..., 2] * w2) / (w0 + w1 + w2)
+
+
 def ivpsnr_db(sse, area, w_avg=(4, 1, 1)):
     """IV-PSNR per image from the [n, 2, 3] SSE: min over directions of the weighted
     10 log10(area / SSE_c) (Max = 1; xIVPSNR.cpp:100-133)."""
-    w = torch.tensor(w_avg, dtype=sse.dtype, device=sse.device)
-    q = (10.0 * torch.log10(area / sse) * w).sum(-1) / w.sum()
-    return q.min(dim=1).values
+    return _wmean(10.0 * torch.log10(area / sse), w_avg).min(dim=1).values
 
 
 def ivssim(ssim, w_avg=(4, 1, 1)):
     """IV-SSIM per image from the [n, 2, 3] SSIM values: min over directions of the weighted
     mean (xSSIM.cpp:192-210)."""
-    w = torch.tensor(w_avg, dtype=ssim.dtype, device=ssim.device)
-    return ((ssim * w).sum(-1) / w.sum()).min(dim=1).values
+    return _wmean(ssim, w_avg).min(dim=1).values
