@@ -64,12 +64,14 @@ def test_range_check_matches_reference(gpu_lib, oq, case):
     assert list(cnt) == [0, 0, 0]
 
 
-@pytest.mark.parametrize("cf,bd", [(420, 8), (422, 10), (444, 10)])
-def test_yuv_reader_feeds_the_metrics(gpu_lib, oq, tmp_path, cf, bd):
+# the last case's frames (1.6 MiB) take the reader's parallel slice reads (frames of 1 MiB and
+# more), the others a single read
+@pytest.mark.parametrize("cf,bd,w,h", [(420, 8, 96, 64), (422, 10, 96, 64), (444, 10, 96, 64), (420, 10, 1024, 544)])
+def test_yuv_reader_feeds_the_metrics(gpu_lib, oq, tmp_path, cf, bd, w, h):
     import torch
     from ivpsnr_gb300 import _abi
     lib = _abi.load()
-    w, h, nf = 96, 64, 3
+    nf = 3
     frames = []
     for f in range(nf):
         r, t = synth.pair420(w, h, bd, seed=70 + f, holes=True)
