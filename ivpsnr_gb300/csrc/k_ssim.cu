@@ -624,11 +624,21 @@ __global__ void __launch_bounds__(kFinThreads) k_ssim_finalize(const SsimJob* __
   {
     const float* pr = J.partial + (int64_t)r * J.tiles_x;
     float hi = 0.0f, lo = 0.0f;
-    for(int t = 0; t < J.tiles_x; t++)
+    // eight loads in flight ahead of the (serial) pair additions, in the same order
+    constexpr int kB = 8;
+    for(int t0 = 0; t0 < J.tiles_x; t0 += kB)
     {
-      float e;
-      fin_two_sum(hi, __ldcg(pr + t), hi, e);
-      lo = __fadd_rn(lo, e);
+      float v[kB];
+      #pragma unroll
+      for(int j = 0; j < kB; j++) v[j] = t0 + j < J.tiles_x ? __ldcg(pr + t0 + j) : 0.0f;
+      #pragma unroll
+      for(int j = 0; j < kB; j++)
+      {
+        if(t0 + j >= J.tiles_x) break;
+        float e;
+        fin_two_sum(hi, v[j], hi, e);
+        lo = __fadd_rn(lo, e);
+      }
     }
     k = kbns_add(k, __dadd_rn((double)hi, (double)lo));
   }
