@@ -144,3 +144,48 @@ def test_input_side_rejections(gpu_lib, tmp_path):
         assert lib.qmiv_yuv_read(r, 1000 // 48, ctypes.byref(out), None) != 0
     finally:
         lib.qmiv_yuv_close(r)
+
+
+def test_range_check_from_several_threads(gpu_lib):
+    """qmiv_check_range keeps its counters per calling thread and device: four host threads
+    checking different pictures at once (ctypes releases the GIL) each get their own counts,
+    also on their first call, when the counters are made."""
+    import threading
+
+    import torch
+    from ivpsnr_gb300 import _abi
+    lib = _abi.load()
+    w, h, bd = 256, 64, 10
+    rng = np.random.default_rng(11)
+    pics, want = [], []
+    for k in range(4):
+        planes = [rng.integers(0, 1 << bd, (h, w)).astype(np.uint16) for _ in range(3)]
+        for c in range(3):  # k + c + 1 samples above 1023 in component c of picture k
+            idx = rng.choice(w * h, size=k + c + 1, replace=False)
+            planes[c].reshape(-1)[idx] = 1023 + 1 + rng.integers(0, 100, size=idx.size)
+        pic, keep = _dev_pic(gpu_lib, planes, bd, gpu_lib.CF444)
+        pics.append((pic, keep))
+        want.append([k + 1, k + 2, k + 3])
+    torch.cuda.synchronize()
+    got = [None] * 4
+    errors = []
+
+    def work(k):
+        try:
+            torch.cuda.set_device(0)
+            for _ in range(20):
+                cnt = (ctypes.c_int64 * 3)()
+                _abi.check(lib.qmiv_check_range(ctypes.byref(pics[k][0]), 0, cnt, None), "qmiv_check_range")
+                if list(cnt) != want[k]:
+                    errors.append((k, list(cnt)))
+            got[k] = list(cnt)
+        except Exception as ex:  # reported below, not swallowed
+            errors.append((k, repr(ex)))
+
+    threads = [threading.Thread(target=work, args=(k,)) for k in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    assert got == want
