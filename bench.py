@@ -238,6 +238,8 @@ def ssim_workload(args, dev, stream):
     px = w * h * nf
     return {"workload": SSIM_WORKLOAD, "value": px / (ms * 1e-3) / 1e9, "unit": "Gpixel/s", "ms_per_step": ms,
             "plain_value": px / (plain_ms * 1e-3) / 1e9, "batched_over_plain": plain_ms / ms, "kernel_ms": kt,
+            # the fused kernel's window positions: every component of every frame at luma resolution
+            "quad_outputs": nf * 3 * max(0, w - 10) * max(0, h - 10),
             "check": {"ivssim_frame0": r0.ivssim, "ssim_frame0": list(r0.ssim)[:3]}}
 
 
@@ -736,6 +738,19 @@ def run_ours(args):
             "check": {"ivpsnr_pair0": r0.ivpsnr, "gcd_pair0": list(r0.gcd_r2t)[:3]},
         }
         if ssim_line:
+            # FP32 view of the fused SSIM kernel: per window position, two separable passes of
+            # 10 taps over 10 moment streams (400 flop), the stream products and four index
+            # evaluations, about 500 flop; peak = FP32 lanes x 2 flop x the sampled clock
+            qk = [k for k in ssim_line.get("kernel_ms", {}) if k.startswith("k_ssim_quad")]
+            if qk and ssim_line["kernel_ms"][qk[0]] > 0:
+                qms = ssim_line["kernel_ms"][qk[0]]
+                fl = 500.0 * ssim_line["quad_outputs"]
+                fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6
+                ssim_line["roofline_fp32"] = {
+                    "kernel": qk[0], "bound": "fp32 pipe", "flop_per_output": 500, "outputs": ssim_line["quad_outputs"],
+                    "kernel_ms": qms, "achieved_tflops": fl / (qms * 1e-3) / 1e12, "peak_tflops": fp32_peak / 1e12,
+                    "frac": fl / (qms * 1e-3) / fp32_peak,
+                    "peak_kind": "152 SMs x 128 FP32 lanes x 2 flop x sampled SM clock"}
             line["ivssim"] = ssim_line
         if loss_line:
             line["loss"] = loss_line
