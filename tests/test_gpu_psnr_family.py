@@ -62,6 +62,11 @@ CASES = [
     (6, 4, 8, 12, False, {}),
     (64, 64, 10, 13, False, {"cmp_w_search": (1, 1, 1), "cmp_w_avg": (1, 1, 1)}),
     (64, 64, 10, 14, False, {"cmp_w_search": (3, 2, 1)}),
+    # search ranges the specialised kernels do not take (generic kernel): none, and 5 to 16
+    (96, 64, 10, 15, True, {"search_range": 0}),
+    (120, 72, 10, 16, True, {"search_range": 5}),
+    (128, 80, 8, 17, True, {"search_range": 8}),
+    (160, 96, 10, 18, True, {"search_range": 16}),
 ]
 
 

@@ -20,11 +20,11 @@ def _planes(flat, w, h, dtype=np.uint16):
     return [np.ascontiguousarray(p.astype(dtype)) for p in synth.split420(flat, w, h)]
 
 
-def _oracle(oq, ref, tst, w, h, bd, window=0):
+def _oracle(oq, ref, tst, w, h, bd, window=0, search_range=2):
     from oracle.oracle import upsample420
     p0 = upsample420(synth.split420(ref, w, h), w, h)
     p1 = upsample420(synth.split420(tst, w, h), w, h)
-    return oq.frame(p0, p1, bd, True, ssim_window=window, nthreads=8), p0, p1
+    return oq.frame(p0, p1, bd, True, ssim_window=window, search_range=search_range, nthreads=8), p0, p1
 
 
 def _cmp_ssim(g, o):
@@ -55,6 +55,20 @@ def test_frame_ssim_family(gpu_lib, oq, w, h, bd, seed, holes, window):
     with gpu_lib.Processor(w, h, ssim_window=window) as P:
         g = P.calc_frame(gpu_lib.make_pic(_planes(ref, w, h, dtype), bd), gpu_lib.make_pic(_planes(tst, w, h, dtype), bd),
                          gpu_lib.M_ALL)
+    _cmp_ssim(g, o)
+    assert g["gcd_r2t"][:3] == o["gcd"]
+    assert abs(g["ivpsnr"] - o["ivpsnr"]) <= 1e-10
+
+
+@pytest.mark.parametrize("sr", [0, 6])
+def test_ivssim_with_generic_search(gpu_lib, oq, sr):
+    """IV-SSIM from shift-compensated pictures of the generic search kernel (search ranges the
+    specialised kernels do not take)."""
+    w, h, bd = 144, 96, 10
+    ref, tst = synth.pair420(w, h, bd, seed=140 + sr, holes=True)
+    o, _, _ = _oracle(oq, ref, tst, w, h, bd, search_range=sr)
+    with gpu_lib.Processor(w, h, search_range=sr) as P:
+        g = P.calc_frame(gpu_lib.make_pic(_planes(ref, w, h), bd), gpu_lib.make_pic(_planes(tst, w, h), bd), gpu_lib.M_ALL)
     _cmp_ssim(g, o)
     assert g["gcd_r2t"][:3] == o["gcd"]
     assert abs(g["ivpsnr"] - o["ivpsnr"]) <= 1e-10
