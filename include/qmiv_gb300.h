@@ -212,7 +212,8 @@ qmiv_status qmiv_psnr(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1
  * all handed to one caching allocator up front, and that have nowhere to keep a handle.
  * It runs a variant of the statistics kernel whose scratch (per-row sums, the block counter
  * and the result) is one static device array of about 385 KiB; pictures taller than 8192
- * rows are rejected with QMIV_TOO_LARGE, host pictures with QMIV_BAD_ARG. opt may be null
+ * rows or wider than 65536 samples are rejected with QMIV_TOO_LARGE, host pictures with
+ * QMIV_BAD_ARG. opt may be null
  * (defaults); it supplies unnoticeable, cmp_w_avg and fake_exact. Fills out->psnr,
  * psnr_pic, gcd_r2t and exact; every other field is 0. Synchronous on `stream`.
  * The first call on each device looks up the static array's address and should be made
@@ -228,6 +229,18 @@ qmiv_status qmiv_ivpsnr(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pi
 qmiv_status qmiv_scp(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, const int32_t* gcd_r2t,
                      uint16_t* scp0[3], uint16_t* scp1[3], int32_t scp_stride, int32_t scp_is_device,
                      qmiv_stream stream);
+/* The corresponding-pixel search itself, pixel by pixel: for every pixel of both directions the
+ * window index (dy + B)(2B + 1) + (dx + B) of the candidate that
+ * xCorrespPixelShift::xFindBestPixelWithinBlock returns (xCorrespPixelShift.cpp:48-85, the first
+ * strict minimum in row-major order; R2T searches picture 1 for picture 0 + GCD, T2R picture 0
+ * for picture 1 - GCD), as int16 maps of width x height with row pitch map_stride (host or device
+ * per map_is_device). row_sse (host, may be null) receives the per-row squared errors at the
+ * argmin, [2][height][3] for R2T then T2R and Y, Cb, Cr (xCorrespPixelShift::xCalcDistAsymmetricRow,
+ * xCorrespPixelShift.cpp:20-46). gcd_r2t may be null (computed). Synchronous. Host outputs use a
+ * device buffer of 4 * max_width * max_height bytes that the handle allocates on first use. */
+qmiv_status qmiv_cps_maps(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, const int32_t* gcd_r2t,
+                          int16_t* map_r2t, int16_t* map_t2r, int32_t map_stride, int32_t map_is_device,
+                          uint64_t* row_sse, qmiv_stream stream);
 /* xSSIM::calcPicSSIM(Tst, Ref, CalcL) (xSSIM.cpp:54) on any two pictures (e.g. P0 and SCP1) */
 qmiv_status qmiv_ssim(qmiv_handle* h, const qmiv_pic* tst, const qmiv_pic* ref, int32_t calc_l, double ssim[4],
                       qmiv_stream stream);

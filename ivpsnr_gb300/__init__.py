@@ -7,6 +7,8 @@ and calls the C ABI; every metric is computed by the CUDA kernels.
 """
 import ctypes
 
+import numpy as np
+
 from . import _abi
 from ._abi import (CF420, CF444, M_ALL, M_IVPSNR, M_IVSSIM, M_MSSSIM, M_PSNR, M_SSIM, M_WSPSNR, QmivError,
                    SSIM_GAUSS11, SSIM_REF10)
@@ -147,6 +149,19 @@ class Processor:
         stride = _ptr_and_stride(scp0[0])[1]
         _abi.check(self.lib.qmiv_scp(self.h, ctypes.byref(pic0), ctypes.byref(pic1), g, a0, a1, stride,
                                      int(is_device), stream), "qmiv_scp")
+
+    def cps_maps(self, pic0, pic1, gcd=None, stream=0):
+        """qmiv_cps_maps with host outputs: (map_r2t, map_t2r) int16 (H, W) window indices
+        (dy + B)(2B + 1) + (dx + B) of each pixel's argmin, and the per-row squared errors at the
+        argmin, uint64 (2, H, 3)."""
+        w, h = pic0.width, pic0.height
+        m0 = np.zeros((h, w), np.int16)
+        m1 = np.zeros((h, w), np.int16)
+        rows = np.zeros((2, h, 3), np.uint64)
+        g = (ctypes.c_int32 * 4)(*(list(gcd) + [0] * (4 - len(gcd)))) if gcd is not None else None
+        _abi.check(self.lib.qmiv_cps_maps(self.h, ctypes.byref(pic0), ctypes.byref(pic1), g, m0.ctypes.data,
+                                          m1.ctypes.data, w, 0, rows.ctypes.data, stream), "qmiv_cps_maps")
+        return m0, m1, rows
 
     def calc_batch(self, jobs, results_ptr, stream=0):
         arr = (_abi.Job * len(jobs))(*jobs)

@@ -85,6 +85,7 @@ SIGNATURES = [
     ("qmiv_psnr_static", c_i32, [_P(Pic), _P(Pic), _P(Options), _P(FrameResult), _vp]),
     ("qmiv_ivpsnr", c_i32, [_vp, _P(Pic), _P(Pic), _P(c_i32), _P(c_f64), _P(c_f64), _P(c_f64), _vp]),
     ("qmiv_scp", c_i32, [_vp, _P(Pic), _P(Pic), _P(c_i32), _P(_vp), _P(_vp), c_i32, c_i32, _vp]),
+    ("qmiv_cps_maps", c_i32, [_vp, _P(Pic), _P(Pic), _P(c_i32), _vp, _vp, c_i32, c_i32, _vp, _vp]),
     ("qmiv_ssim", c_i32, [_vp, _P(Pic), _P(Pic), c_i32, _P(c_f64), _vp]),
     ("qmiv_msssim", c_i32, [_vp, _P(Pic), _P(Pic), _P(c_f64), _vp]),
     ("qmiv_ivssim", c_i32, [_vp, _P(Pic), _P(Pic), _P(c_i32), _P(c_f64), _P(c_f64), _P(c_f64), _vp]),

@@ -81,6 +81,7 @@ k_cps420(const DevJob* __restrict__ jobs, int njobs, Params p)
   const int cyBase = (y0 >> 1) - G::CS;
   uint16_t* const* scp = dir == 0 ? J.scp1 : J.scp0;
   const bool want_scp = scp[0] != nullptr;
+  int16_t* const cmap = J.cps_map[dir];
 
   unsigned int sse[RPT][3];
   #pragma unroll
@@ -219,6 +220,7 @@ k_cps420(const DevJob* __restrict__ jobs, int njobs, Params p)
         else                       { rY = rl / s; tYr = tY[i][px] / s; }
         const int d0 = tYr - rY, d1 = tCb[i >> 1] - rcb, d2 = tCr[i >> 1] - rcr;
         sse[i][0] += (unsigned)(d0 * d0); sse[i][1] += (unsigned)(d1 * d1); sse[i][2] += (unsigned)(d2 * d2);
+        if(cmap) cmap[(int64_t)y * J.map_stride + x] = (int16_t)k;  // window index (dy + B)(2B + 1) + (dx + B)
         if(want_scp)
         { // clipU(ref - GCD) (xShftCompPic.cpp:88-92); for T2R the shift is -GCD
           const int v0 = clampi(rY - gd0, 0, mx), v1 = clampi(rcb - gd1, 0, mx), v2 = clampi(rcr - gd2, 0, mx);
@@ -278,7 +280,7 @@ __global__ void __launch_bounds__(kGenTX * kGenTY * 2) k_cps_generic(const DevJo
   {
     long long tv[3];
     for(int c = 0; c < 3; c++) tv[c] = ld_pel(J, tp, c, x, y) + gd[c];
-    long long bestE = LLONG_MAX; int bx = x, by = y;
+    long long bestE = LLONG_MAX; int bx = x, by = y, bk = 0;
     for(int dy = -SR; dy <= SR; dy++)
     {
       const int yy = clampi(y + dy, 0, H - 1);
@@ -287,9 +289,10 @@ __global__ void __launch_bounds__(kGenTX * kGenTY * 2) k_cps_generic(const DevJo
         const int xx = clampi(x + dx, 0, W - 1);
         long long E = 0;
         for(int c = 0; c < 3; c++) { const long long d = tv[c] - ld_pel(J, rp, c, xx, yy); E += d * d * p.w_search[c]; }
-        if(E < bestE) { bestE = E; bx = xx; by = yy; }
+        if(E < bestE) { bestE = E; bx = xx; by = yy; bk = (dy + SR) * (2 * SR + 1) + dx + SR; }
       }
     }
+    if(J.cps_map[dir]) J.cps_map[dir][(int64_t)y * J.map_stride + x] = (int16_t)bk;
     uint16_t* const* scp = dir == 0 ? J.scp1 : J.scp0;
     for(int c = 0; c < 3; c++)
     {

@@ -91,6 +91,7 @@ k_cps420_tma(const DevJob* __restrict__ jobs, int njobs, Params p)
   const int mx = (1 << J.bd) - 1;
   uint16_t* const* scp = dir == 0 ? J.scp1 : J.scp0;
   const bool want_scp = scp[0] != nullptr;
+  int16_t* const cmap = J.cps_map[dir];
   const int cry0 = (y0 >> 1) - G::CS;
 
   for(int i = tid; i < 2 * G::R * 3; i += G::NT) acc[i] = 0ull;
@@ -375,6 +376,11 @@ k_cps420_tma(const DevJob* __restrict__ jobs, int njobs, Params p)
               sq[a][0] += (unsigned)(d0 * d0) & vm; sq[a][1] += (unsigned)(d1 * d1) & vm; sq[a][2] += (unsigned)(d2 * d2) & vm;
             }
             sv[a][px][0] = rY; sv[a][px][1] = rcb; sv[a][px][2] = rcr;
+            if(cmap && (IN || (yq + a < H && cx0 + 2 * lane + px < W)))
+            { // the reference's window index (dy + B)(2B + 1) + (dx + B)
+              cmap[(int64_t)(yq + a) * J.map_stride + cx0 + 2 * lane + px] =
+                  (int16_t)((int)(k >> G::KS_LOG2) * W2 + (int)(k & (G::KS - 1)));
+            }
           }
         if(want_scp)
         { // clipU(ref - GCD) (xShftCompPic.cpp:88-92); for T2R the shift is -GCD

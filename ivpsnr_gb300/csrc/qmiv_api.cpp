@@ -160,6 +160,8 @@ struct qmiv_handle {
   int64_t* mask_rows = nullptr;
   uint8_t* mask_small = nullptr;
   uint16_t* mask_stage = nullptr;
+  // qmiv_cps_maps with host outputs: both directions' argmin maps (sized on first use)
+  int16_t* d_maps = nullptr;
   std::map<std::pair<int, int>, std::pair<double*, double>> ws_cache;
   SeqAcc seq;
   int64_t launches = 0;
@@ -1108,6 +1110,7 @@ qmiv_status qmiv_destroy(qmiv_handle* h)
   cudaFree(h->mask_rows);
   cudaFree(h->mask_small);
   cudaFree(h->mask_stage);
+  cudaFree(h->d_maps);
   for(auto& kv : h->ws_cache) cudaFree(kv.second.first);
   for(auto& p : h->prof) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
   delete h;
@@ -1168,7 +1171,8 @@ qmiv_status qmiv_set_cps_variant(qmiv_handle* h, int32_t v)
 // ------------------------------------------------------------------------------------
 static qmiv_status frame_common(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, uint32_t metrics,
                                 const int32_t* gcd_given, uint16_t* const* scp0, uint16_t* const* scp1, int32_t scp_stride,
-                                qmiv_frame_result* out, cudaStream_t st)
+                                qmiv_frame_result* out, cudaStream_t st, int16_t* map_r2t = nullptr,
+                                int16_t* map_t2r = nullptr, int32_t map_stride = 0)
 {
   if(!h) return fail(QMIV_BAD_ARG, "handle is null");
   qmiv_status s = check_pair(h, pic0, pic1);
@@ -1189,6 +1193,9 @@ static qmiv_status frame_common(qmiv_handle* h, const qmiv_pic* pic0, const qmiv
     for(int c = 0; c < 3; c++) { j.scp0[c] = h->slots[0].scp + c * area; j.scp1[c] = h->slots[0].scp + (3 + c) * area; }
     j.scp_stride = j.W;
   }
+  j.cps_map[0] = map_r2t;
+  j.cps_map[1] = map_t2r;
+  j.map_stride = map_stride;
   if(gcd_given)
   {
     int32_t g[4] = { gcd_given[0], gcd_given[1], gcd_given[2], 0 };
@@ -1320,6 +1327,8 @@ qmiv_status qmiv_psnr_static(const qmiv_pic* pic0, const qmiv_pic* pic1, const q
     if(p->width < 1 || p->height < 1) return fail(QMIV_BAD_ARG, "pic%d: size %dx%d", i, p->width, p->height);
     if(p->height > kStaticMaxRows)
       return fail(QMIV_TOO_LARGE, "pic%d: height %d exceeds the static scratch limit of %d rows", i, p->height, kStaticMaxRows);
+    if(p->width > kStaticMaxWidth)
+      return fail(QMIV_TOO_LARGE, "pic%d: width %d exceeds the limit of %d samples per row", i, p->width, kStaticMaxWidth);
     if(p->bitdepth < 1 || p->bitdepth > 14) return fail(QMIV_BAD_ARG, "pic%d: bit depth %d (1..14)", i, p->bitdepth);
     if(p->sample_bytes != 1 && p->sample_bytes != 2) return fail(QMIV_BAD_ARG, "pic%d: sample_bytes %d", i, p->sample_bytes);
     if(p->sample_bytes == 1 && p->bitdepth > 8) return fail(QMIV_BAD_ARG, "pic%d: %d-bit samples in 8-bit storage", i, p->bitdepth);
@@ -1407,6 +1416,36 @@ qmiv_status qmiv_scp(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1,
     CUDA_TRY(cudaMemcpy2DAsync(scp0[c], (size_t)scp_stride * 2, d0[c], (size_t)pic0->width * 2, (size_t)pic0->width * 2, pic0->height, cudaMemcpyDeviceToHost, st));
     CUDA_TRY(cudaMemcpy2DAsync(scp1[c], (size_t)scp_stride * 2, d1[c], (size_t)pic0->width * 2, (size_t)pic0->width * 2, pic0->height, cudaMemcpyDeviceToHost, st));
   }
+  CUDA_TRY(cudaStreamSynchronize(st));
+  return QMIV_OK;
+}
+
+qmiv_status qmiv_cps_maps(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1, const int32_t* gcd,
+                          int16_t* map_r2t, int16_t* map_t2r, int32_t map_stride, int32_t map_is_device, uint64_t* row_sse,
+                          qmiv_stream stream)
+{
+  if(!h) return fail(QMIV_BAD_ARG, "handle is null");
+  if(!map_r2t || !map_t2r) return fail(QMIV_BAD_ARG, "map outputs are null");
+  if(!pic0) return fail(QMIV_BAD_ARG, "pic0 is null");
+  if(map_stride < pic0->width) return fail(QMIV_BAD_ARG, "map_stride %d < width %d", map_stride, pic0->width);
+  cudaStream_t st = (cudaStream_t)stream;
+  qmiv_frame_result r;
+  qmiv_status s;
+  const int W = pic0->width, H = pic0->height;
+  if(map_is_device) s = frame_common(h, pic0, pic1, QMIV_M_IVPSNR, gcd, nullptr, nullptr, 0, &r, st, map_r2t, map_t2r, map_stride);
+  else
+  {
+    if(!h->d_maps) CUDA_TRY(cudaMalloc(&h->d_maps, (size_t)2 * h->max_w * h->max_h * sizeof(int16_t)));
+    int16_t* d0 = h->d_maps;
+    int16_t* d1 = h->d_maps + (size_t)h->max_w * h->max_h;
+    s = frame_common(h, pic0, pic1, QMIV_M_IVPSNR, gcd, nullptr, nullptr, 0, &r, st, d0, d1, W);
+    if(s != QMIV_OK) return s;
+    CUDA_TRY(cudaMemcpy2DAsync(map_r2t, (size_t)map_stride * 2, d0, (size_t)W * 2, (size_t)W * 2, H, cudaMemcpyDeviceToHost, st));
+    CUDA_TRY(cudaMemcpy2DAsync(map_t2r, (size_t)map_stride * 2, d1, (size_t)W * 2, (size_t)W * 2, H, cudaMemcpyDeviceToHost, st));
+  }
+  if(s != QMIV_OK) return s;
+  if(row_sse)
+    CUDA_TRY(cudaMemcpyAsync(row_sse, h->slots[0].cps_rows, (size_t)2 * H * 3 * sizeof(uint64_t), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaStreamSynchronize(st));
   return QMIV_OK;
 }

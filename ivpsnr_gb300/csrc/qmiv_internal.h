@@ -33,6 +33,8 @@ struct DevJob {
   uint16_t* scp0[3];                  // built from picture 0 (T2R argmin), may be null
   uint16_t* scp1[3];                  // built from picture 1 (R2T argmin), may be null
   int32_t scp_stride;
+  int16_t* cps_map[2];                // argmin window index per pixel, R2T then T2R; may be null
+  int32_t map_stride;
   int32_t gcd_given;                  // 1: sc->gcd preset by the host, stats kernel leaves it
   int32_t slot;                       // the handle's scratch slot (host bookkeeping)
   const void* tmaps;                  // 6 tensor maps (picture 0 Y,Cb,Cr then picture 1) or null
@@ -68,6 +70,9 @@ cudaError_t launch_stats(const DevJob* d_jobs, const DevJob* h_jobs, int n, cons
 
 // Statistics of one picture pair in a static device array (k_stats.cu): no allocation.
 constexpr int kStaticMaxRows = 8192;     // tallest picture the static row sums hold
+// widest picture of the static path: a row's sum of differences is kept in an int32, and
+// 65536 samples x (2^14 - 1) stays below 2^31 at every supported bit depth
+constexpr int kStaticMaxWidth = 65536;
 constexpr int kStaticMaxDevices = 64;
 
 // Launch attributes (cudaFuncSetAttribute, occupancy) belong to the current device, so the

@@ -14,11 +14,12 @@
 # On x86-64 the build targets x86-64-v4 (the level the reference's runtime dispatcher
 # picks on AVX-512 hosts); elsewhere it builds the portable STD code paths.
 #
-# Usage: oracle/build_ref.sh [REFERENCE_SOURCE_DIR]   (default /root/reference)
+# Usage: oracle/build_ref.sh [REFERENCE_SOURCE_DIR]   (default $QMIV_REFERENCE_DIR, else /root/reference)
+# Exits 3 without building when the sources are absent.
 set -euo pipefail
 
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
-SRC="${1:-${QMIV_REF_SRC:-/root/reference}}"
+SRC="${1:-${QMIV_REFERENCE_DIR:-/root/reference}}"
 OUT="$HERE/_ref"
 OBJ="$OUT/obj"
 

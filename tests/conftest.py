@@ -7,7 +7,6 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-REFERENCE = os.environ.get("QMIV_REFERENCE_DIR", "/root/reference")
 
 
 def pytest_configure(config):

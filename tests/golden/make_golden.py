@@ -167,9 +167,24 @@ def run_case(name, w, h, bd, seed, gkw, hopt, tmp):
     }
 
 
+def write_ssim_window(src=None):
+    """tests/golden/ssim_window.json: the reference's 10x10 SSIM window table (c_FilterF,
+    libs/pmbb-ivqm/src/xStructSimConsts.h:31-44) as the FP32 values its source spells out."""
+    import re
+    src = src or os.environ.get("QMIV_REFERENCE_DIR", "/root/reference")
+    txt = open(os.path.join(src, "libs", "pmbb-ivqm", "src", "xStructSimConsts.h")).read()
+    vals = [float(v) for v in re.findall(r"([0-9]\.[0-9]+)f", txt)][:121]
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "ssim_window.json")
+    with open(path, "w") as f:
+        json.dump({"source": "libs/pmbb-ivqm/src/xStructSimConsts.h:31-44 (c_FilterF, 11x11 storage, 10x10 used)",
+                   "values": vals}, f)
+    print("wrote", path)
+
+
 def main():
     if not os.path.exists(HARNESS):
         sys.exit("build the reference first: oracle/build_ref.sh")
+    write_ssim_window()
     tmp = tempfile.mkdtemp()
     cases = [run_case(*c, tmp) for c in CASES]
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "cases.json")

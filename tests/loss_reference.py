@@ -38,8 +38,9 @@ def _gather(stack, k):
     return torch.gather(stack, 2, k[:, None, None].expand(n, c, 1, h, w)).squeeze(2)
 
 
-def ssim(x, y, win=10, c1=1e-4, c2=9e-4):
-    """Picture SSIM of each plane pair of [n, 3, H, W] tensors -> [n, 3] (L*CS, Max = 1)."""
+def ssim_map(x, y, win=10, c1=1e-4, c2=9e-4):
+    """Per-position SSIM L*CS of each plane pair of [n, 3, H, W] tensors over the valid region
+    [5, H-5) x [5, W-5) -> [n, 3, H-10, W-10] (Max = 1)."""
     n, c, h, w = x.shape
     g = window_factor(win).to(x.dtype).to(x.device)
     k2 = torch.outer(g, g)[None, None].expand(c, 1, win, win)
@@ -47,12 +48,29 @@ def ssim(x, y, win=10, c1=1e-4, c2=9e-4):
     mx, my = conv(x), conv(y)
     exx, eyy, exy = conv(x * x), conv(y * y), conv(x * y)
     vx, vy, cov = exx - mx * mx, eyy - my * my, exy - mx * my
-    s = ((2 * mx * my + c1) / (mx * mx + my * my + c1)) * ((2 * cov + c2) / (vx + vy + c2))
-    return s.sum(dim=(2, 3)) / (h * w)
+    return ((2 * mx * my + c1) / (mx * mx + my * my + c1)) * ((2 * cov + c2) / (vx + vy + c2))
+
+
+def ssim(x, y, win=10, c1=1e-4, c2=9e-4):
+    """Picture SSIM of each plane pair of [n, 3, H, W] tensors -> [n, 3] (L*CS, Max = 1)."""
+    h, w = x.shape[-2:]
+    return ssim_map(x, y, win, c1, c2).sum(dim=(2, 3)) / (h * w)
 
 
 def forward(tst, ref, sr=2, w_search=(4.0, 1.0, 1.0), unc=(0.01, 0.01, 0.01), win=10):
     """(sse[n, 2, 3], ssim[n, 2, 3]) in tst's dtype; differentiable with respect to tst."""
+    e1, e0, s_r2t, s_t2r, ks = forward_maps(tst, ref, sr, w_search, unc, win)
+    h, w = tst.shape[-2:]
+    sse = torch.stack([(e1 * e1).sum(dim=(2, 3)), (e0 * e0).sum(dim=(2, 3))], dim=1)
+    ss = torch.stack([s_r2t.sum(dim=(2, 3)), s_t2r.sum(dim=(2, 3))], dim=1) / (h * w)
+    return sse, ss, ks
+
+
+def forward_maps(tst, ref, sr=2, w_search=(4.0, 1.0, 1.0), unc=(0.01, 0.01, 0.01), win=10):
+    """The terms before their picture sums: the R2T and T2R errors at the argmin [n, 3, H, W], the
+    per-position SSIM of both directions [n, 3, H-10, W-10], and the argmin maps. Differences of
+    two evaluations are taken term by term before summing, which keeps central differences of the
+    picture sums free of the summation's rounding at large sizes."""
     dt = tst.dtype
     n, _, h, w = tst.shape
     m = (ref.double() - tst.double()).mean(dim=(2, 3)).to(dt)
@@ -71,8 +89,6 @@ def forward(tst, ref, sr=2, w_search=(4.0, 1.0, 1.0), unc=(0.01, 0.01, 0.01), wi
     d0_32 = (ref.float() - g4.float()).unsqueeze(2) - ts.float()
     k0 = _werr(d0_32, wt).argmin(dim=1)
     e0 = _gather(d0, k0)
-    sse = torch.stack([(e1 * e1).sum(dim=(2, 3)), (e0 * e0).sum(dim=(2, 3))], dim=1)
     scp1 = torch.clamp(_gather(rs, k1) - g4, 0.0, 1.0)
     scp0 = torch.clamp(_gather(ts, k0) + g4, 0.0, 1.0)
-    ss = torch.stack([ssim(ref, scp0, win), ssim(tst, scp1, win)], dim=1)
-    return sse, ss, (k1, k0)
+    return e1, e0, ssim_map(ref, scp0, win), ssim_map(tst, scp1, win), (k1, k0)

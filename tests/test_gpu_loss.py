@@ -153,3 +153,71 @@ def test_loss_helpers(gpu_lib):
     assert torch.allclose(loss.ivssim(ss).cpu(), ((ss.cpu() * w).sum(-1) / 6).min(dim=1).values)
     with pytest.raises(ValueError):
         loss.iv_metrics(tst.cuda().double(), ref.cuda().double())
+
+
+def test_config3_full_size_against_fp64(gpu_lib):
+    """The differentiable workload at its own size: 16 FP32 4:4:4 pictures of 1024x1024 in one
+    forward and backward, every value and gradient against the FP64 restatement on the GPU (two
+    pictures at a time: each picture's terms depend on that picture only), same bars as above."""
+    import torch
+    n, w, h = 16, 1024, 1024
+    tst, ref = _pair(n, w, h, 61)
+    a, b = _loss_weights(n, 61)
+    g_sse, g_ss, g_grad = _gpu(tst, ref, a, b)
+    for i in range(0, n, 2):
+        sl = slice(i, i + 2)
+        r_sse, r_ss, r_grad, _ = _ref(tst[sl].cuda(), ref[sl].cuda(), a[sl].cuda(), b[sl].cuda(), torch.float64)
+        r_sse, r_ss, r_grad = r_sse.cpu(), r_ss.cpu(), r_grad.cpu()
+        np.testing.assert_allclose(g_sse[sl].numpy(), r_sse.numpy(), rtol=2e-5, atol=0)
+        np.testing.assert_allclose(g_ss[sl].numpy(), r_ss.numpy(), rtol=0, atol=2e-6)
+        err = (g_grad[sl] - r_grad).abs()
+        scale = r_grad.abs().max().item()
+        assert (err <= 1e-4 * r_grad.abs() + 1e-4 * scale).float().mean().item() == 1.0, (i, err.max().item(), scale)
+        assert torch.linalg.norm(g_grad[sl] - r_grad) <= 1e-4 * torch.linalg.norm(r_grad), i
+        del r_grad, err
+        torch.cuda.empty_cache()
+
+
+def test_config3_central_differences_at_full_size(gpu_lib):
+    """FP64 central differences (h = 1e-4) of the restatement at 64 random (pixel, component)
+    points of a 1024x1024 picture of the batch, against the GPU gradient, 1e-4 relative. The loss
+    difference is summed term by term (errors and per-position SSIM of the two evaluations
+    subtracted before the picture sums), so that rounding in million-term sums does not swamp a
+    change of order 1e-10. Points where the perturbation moves an argmin are skipped."""
+    import torch
+    n, w, h = 2, 1024, 1024
+    tst, ref = _pair(n, w, h, 71)
+    a, b = _loss_weights(n, 71)
+    _, _, g_grad = _gpu(tst, ref, a, b)
+    area = w * h
+    t64, r64 = tst[:1].double().cuda(), ref[:1].double().cuda()
+    a0, b0 = a[0].double().cuda(), b[0].double().cuda()
+    hstep = 1e-4
+
+    def terms(t):
+        with torch.no_grad():
+            return ref_impl.forward_maps(t, r64)
+
+    _, _, _, _, ks0 = terms(t64)
+    rng = np.random.default_rng(9)
+    fd, an, tried = [], [], 0
+    while len(fd) < 64:
+        tried += 1
+        assert tried < 1000, "too few smooth points"
+        y, x, c = int(rng.integers(0, h)), int(rng.integers(0, w)), int(rng.integers(0, 3))
+        tp = t64.clone(); tp[0, c, y, x] += hstep
+        tm = t64.clone(); tm[0, c, y, x] -= hstep
+        p, m = terms(tp), terms(tm)
+        if any(not torch.equal(u, v) for u, v in zip(p[4] + m[4], ks0 + ks0)):
+            continue
+        dl = 0.0
+        for d, (ep, em) in enumerate(((p[0], m[0]), (p[1], m[1]))):   # SSE: R2T, T2R
+            dl += float(((ep * ep - em * em).sum(dim=(2, 3))[0] * a0[d]).sum()) / area
+        for d, (sp, sm) in enumerate(((p[2], m[2]), (p[3], m[3]))):   # SSIM: R2T, T2R
+            dl += float(((sp - sm).sum(dim=(2, 3))[0] * b0[d]).sum()) / area
+        fd.append(dl / (2 * hstep))
+        an.append(float(g_grad[0, c, y, x]))
+    fd, an = np.array(fd), np.array(an)
+    floor = 1e-2 * np.sqrt(np.mean(fd ** 2))
+    rel = np.abs(an - fd) / np.maximum(np.abs(fd), floor)
+    assert rel.max() <= 1e-4, (rel.max(), np.argmax(rel))

@@ -106,11 +106,16 @@ def test_444_input_generic_kernel(gpu_lib, oq):
     _cmp(gpu, ora)
 
 
-@pytest.mark.parametrize("variant", range(0, 64))
+N_CPS_VARIANTS = 30  # compiled CPS variants (qmiv_cps_variant_count); checked below
+
+
+def test_cps_variant_count(gpu_lib):
+    assert len(gpu_lib.cps_variants()) == N_CPS_VARIANTS
+
+
+@pytest.mark.parametrize("variant", range(N_CPS_VARIANTS))
 def test_every_cps_variant(gpu_lib, oq, variant):
     names = gpu_lib.cps_variants()
-    if variant >= len(names):
-        pytest.skip("no such variant")
     name = names[variant]
     sr = 2 if variant == 0 else int(name.split("_sr")[1].split("_")[0])
     # 14-bit samples need 64-bit keys at every search range; 8-bit variants read uint8 planes
@@ -126,9 +131,22 @@ def test_every_cps_variant(gpu_lib, oq, variant):
         gpu = P.calc_frame(gpu_lib.make_pic(_planes(ref, w, h, dtype), bd), gpu_lib.make_pic(_planes(tst, w, h, dtype), bd),
                            gpu_lib.M_PSNR | gpu_lib.M_WSPSNR | gpu_lib.M_IVPSNR)
         ran = [n for n, _ in P.kernel_times()]
+        m0, m1, rows = P.cps_maps(gpu_lib.make_pic(_planes(ref, w, h, dtype), bd), gpu_lib.make_pic(_planes(tst, w, h, dtype), bd))
+        ran_maps = [n for n, _ in P.kernel_times()]
     assert name in ran, (name, ran)  # the requested variant is the one that ran
+    assert name in ran_maps, (name, ran_maps)
     _cmp(gpu, ora)
     assert gpu["status"] == 0
+    # per-pixel argmin and per-row sums of both directions, bit-exact
+    from oracle.oracle import upsample420
+    p0 = upsample420(synth.split420(ref, w, h), w, h)
+    p1 = upsample420(synth.split420(tst, w, h), w, h)
+    r0, a0, _, _ = oq.cps_dir(p0, p1, bd, ora["gcd"], sr, nthreads=8)
+    r1, a1, _, _ = oq.cps_dir(p1, p0, bd, [-x for x in ora["gcd"]], sr, nthreads=8)
+    np.testing.assert_array_equal(m0.astype(np.int8), a0)
+    np.testing.assert_array_equal(m1.astype(np.int8), a1)
+    np.testing.assert_array_equal(rows[0], r0)
+    np.testing.assert_array_equal(rows[1], r1)
 
 
 def test_scp_bit_exact(gpu_lib, oq):

@@ -211,3 +211,75 @@ def test_fused_staging_paths_agree(gpu_lib, oq, w, h, bd, cf444, window):
     o = oq.frame(upsample420(synth.split420(ref, w, h), w, h), upsample420(synth.split420(tst, w, h), w, h), bd, True,
                  ssim_window=window, nthreads=8)
     _cmp_ssim(a, o)
+
+
+# ---- the sizes the benchmarks time ---------------------------------------------------------------
+@pytest.mark.parametrize("w,h,sr,ws,window,cfg", [(4096, 2048, 2, True, 0, 1), (7680, 3840, 4, True, 0, 4),
+                                                  (4096, 2048, 2, False, 1, 1)])
+def test_ssim_family_large_planes(gpu_lib, oq, w, h, sr, ws, window, cfg):
+    """SSIM, MS-SSIM (five levels from the full picture) and IV-SSIM on device pictures of the ERP
+    view size of the multiview workload and of the 8K sequence (search range 4), against the oracle
+    (xSSIM.cpp:67-87,192-210): the persistent SSIM kernels' tile walks over large planes."""
+    import torch
+    from oracle.oracle import upsample420
+    ref, tst = synth.pair420(w, h, 10, seed=synth.seed_for(cfg, 0, 0), holes=True)
+    d0 = [torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in synth.split420(ref, w, h)]
+    d1 = [torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in synth.split420(tst, w, h)]
+    with gpu_lib.Processor(w, h, search_range=sr, use_ws=ws, ssim_window=window) as P:
+        g = P.calc_frame(gpu_lib.make_pic(d0, 10), gpu_lib.make_pic(d1, 10), gpu_lib.M_ALL)
+    o = oq.frame(upsample420(synth.split420(ref, w, h), w, h), upsample420(synth.split420(tst, w, h), w, h), 10, True,
+                 use_ws=ws, search_range=sr, ssim_window=window, nthreads=16)
+    _cmp_ssim(g, o)
+    assert g["gcd_r2t"][:3] == o["gcd"]
+    assert g["sse_r2t"][:3] == o["sse_r2t"] and g["sse_t2r"][:3] == o["sse_t2r"]
+    assert abs(g["ivpsnr"] - o["ivpsnr"]) <= 1e-10
+
+
+@pytest.mark.parametrize("window", [0, 1])
+def test_ssim_sequence_of_17_drifting_frames(gpu_lib, oq, window):
+    """The 17-frame SSIM workload (1920x1080 10-bit 4:2:0, block shifts drifting over time) in one
+    batched call, each frame against the oracle, and the per-sequence means of the same frames
+    measured one call per frame (xMetricStat::calcAvgMetric, xAppQMIV.h:256-260) against the
+    compensated mean of the oracle's per-frame values."""
+    import ctypes
+    import torch
+    from ivpsnr_gb300 import _abi
+    from oracle.oracle import upsample420
+    w, h, nf, bd = 1920, 1080, 17, 10
+    jobs, keep, oras, pics = [], [], [], []
+    for f in range(nf):
+        ref, tst = synth.pair420(w, h, bd, seed=synth.seed_for(2, 0, f), drift=True, shift_seed=synth.seed_for(2, 0, 0),
+                                 frame=f)
+        oras.append(oq.frame(upsample420(synth.split420(ref, w, h), w, h), upsample420(synth.split420(tst, w, h), w, h),
+                             bd, True, ssim_window=window, nthreads=16))
+        d0 = [torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in synth.split420(ref, w, h)]
+        d1 = [torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in synth.split420(tst, w, h)]
+        keep += [d0, d1]
+        j = _abi.Job()
+        j.pic0 = gpu_lib.make_pic(d0, bd)
+        j.pic1 = gpu_lib.make_pic(d1, bd)
+        j.metrics = gpu_lib.M_ALL
+        jobs.append(j)
+        pics.append((j.pic0, j.pic1))
+    rs = ctypes.sizeof(_abi.FrameResult)
+    res = torch.zeros(nf * rs, dtype=torch.uint8, device="cuda")
+    with gpu_lib.Processor(w, h, max_jobs=nf, ssim_window=window) as P:
+        P.calc_batch(jobs, res.data_ptr())
+        torch.cuda.synchronize()
+        host = res.cpu().numpy().tobytes()
+        for f, o in enumerate(oras):
+            r = _abi.FrameResult.from_buffer_copy(host[f * rs:(f + 1) * rs]).to_dict()
+            assert r["status"] == 0
+            _cmp_ssim(r, o)
+            assert r["gcd_r2t"][:3] == o["gcd"] and abs(r["ivpsnr"] - o["ivpsnr"]) <= 1e-10
+        for p0, p1 in pics:
+            P.calc_frame(p0, p1, gpu_lib.M_ALL)
+        s = P.finish_sequence()
+    assert s["num_frames"] == nf
+    wv = np.array([4, 1, 1]) / 6.0
+    assert abs(s["ivssim"] - oq.kbns([o["ivssim"] for o in oras]) / nf) <= TOL
+    assert abs(s["ivpsnr"] - oq.kbns([o["ivpsnr"] for o in oras]) / nf) <= 1e-10
+    for c in range(3):
+        assert abs(s["ssim"][c] - oq.kbns([o["ssim"][c] for o in oras]) / nf) <= TOL
+        assert abs(s["msssim"][c] - oq.kbns([o["msssim"][c] for o in oras]) / nf) <= TOL
+    assert abs(s["ssim_pic"] - oq.kbns([float(np.dot(wv, o["ssim"])) for o in oras]) / nf) <= TOL

@@ -6,7 +6,6 @@ oracle/_ref) skip when those are absent.
 """
 import json
 import os
-import re
 import subprocess
 
 import numpy as np
@@ -14,10 +13,10 @@ import pytest
 
 from ivpsnr_gb300 import synth
 
-from .conftest import REFERENCE, ROOT
+from .conftest import ROOT
+from .golden import fencing_io
 
 GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "cases.json")))
-EXAMPLE = os.path.join(REFERENCE, "example")
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "qmiv_ref_harness")
 DB_TOL = 1e-10
 SSIM_TOL = 1e-12  # oracle vs reference are both FP64 (the x86-64-v4 build contracts some FMAs)
@@ -87,11 +86,20 @@ PUBLISHED = [
 
 
 def _load_example(name, w=1920, h=1080):
-    b = np.fromfile(os.path.join(EXAMPLE, name), np.uint8).astype(np.uint16)
-    return _444(b, w, h)
+    """One of the reference's example pictures (committed compressed under tests/golden/fencing/)."""
+    key = name.split("_")[2]
+    return _444(fencing_io.flat(key), w, h)
 
 
-@pytest.mark.skipif(not os.path.isdir(EXAMPLE), reason="reference example pictures not present")
+@pytest.fixture(scope="module")
+def example_dir(tmp_path_factory):
+    """The example pictures as the reference's files, for the reference build's harness."""
+    d = tmp_path_factory.mktemp("example")
+    for key in ("original", "origJpgCompressed", "synthesized", "objectsMask"):
+        fencing_io.write(key, str(d / ("Fencing_v8_%s_1920x1080_yuv420p.yuv" % key)))
+    return str(d)
+
+
 @pytest.mark.parametrize("name,psnr_y,ivpsnr", PUBLISHED)
 def test_oracle_reproduces_published_example(oq, name, psnr_y, ivpsnr):
     p0 = _load_example("Fencing_v8_original_1920x1080_yuv420p.yuv")
@@ -101,7 +109,6 @@ def test_oracle_reproduces_published_example(oq, name, psnr_y, ivpsnr):
     assert round(r["ivpsnr"], 4) == ivpsnr
 
 
-@pytest.mark.skipif(not os.path.isdir(EXAMPLE), reason="reference example pictures not present")
 def test_oracle_reproduces_published_masked_example(oq):
     p0 = _load_example("Fencing_v8_original_1920x1080_yuv420p.yuv")
     p1 = _load_example("Fencing_v8_synthesized_1920x1080_yuv420p.yuv")
@@ -111,10 +118,10 @@ def test_oracle_reproduces_published_masked_example(oq):
     assert round(r["ivpsnr"], 4) == 50.7716
 
 
-@pytest.mark.skipif(not (os.path.isdir(EXAMPLE) and os.path.exists(HARNESS)), reason="reference build not present")
-def test_oracle_matches_reference_on_example_full_precision(oq):
-    a = os.path.join(EXAMPLE, "Fencing_v8_original_1920x1080_yuv420p.yuv")
-    b = os.path.join(EXAMPLE, "Fencing_v8_origJpgCompressed_1920x1080_yuv420p.yuv")
+@pytest.mark.skipif(not os.path.exists(HARNESS), reason="reference build not present")
+def test_oracle_matches_reference_on_example_full_precision(oq, example_dir):
+    a = os.path.join(example_dir, "Fencing_v8_original_1920x1080_yuv420p.yuv")
+    b = os.path.join(example_dir, "Fencing_v8_origJpgCompressed_1920x1080_yuv420p.yuv")
     e = json.loads(subprocess.check_output([HARNESS, "-w", "1920", "-h", "1080", "-bd", "8", "-cf", "420",
                                             "-i0", a, "-i1", b, "-nth", "8"]).decode().splitlines()[0])
     r = oq.frame(_load_example(os.path.basename(a)), _load_example(os.path.basename(b)), 8, True, nthreads=8)
@@ -124,11 +131,11 @@ def test_oracle_matches_reference_on_example_full_precision(oq):
     assert abs(r["ivssim"] - e["ivssim"]) <= SSIM_TOL
 
 
-@pytest.mark.skipif(not (os.path.isdir(EXAMPLE) and os.path.exists(HARNESS)), reason="reference build not present")
-def test_oracle_matches_reference_masked(oq):
-    a = os.path.join(EXAMPLE, "Fencing_v8_original_1920x1080_yuv420p.yuv")
-    b = os.path.join(EXAMPLE, "Fencing_v8_synthesized_1920x1080_yuv420p.yuv")
-    mk = os.path.join(EXAMPLE, "Fencing_v8_objectsMask_1920x1080_yuv420p.yuv")
+@pytest.mark.skipif(not os.path.exists(HARNESS), reason="reference build not present")
+def test_oracle_matches_reference_masked(oq, example_dir):
+    a = os.path.join(example_dir, "Fencing_v8_original_1920x1080_yuv420p.yuv")
+    b = os.path.join(example_dir, "Fencing_v8_synthesized_1920x1080_yuv420p.yuv")
+    mk = os.path.join(example_dir, "Fencing_v8_objectsMask_1920x1080_yuv420p.yuv")
     e = json.loads(subprocess.check_output([HARNESS, "-w", "1920", "-h", "1080", "-bd", "8", "-cf", "420",
                                             "-i0", a, "-i1", b, "-im", mk, "-nth", "8"]).decode().splitlines()[0])
     r = oq.masked(_load_example(os.path.basename(a)), _load_example(os.path.basename(b)),
@@ -140,11 +147,30 @@ def test_oracle_matches_reference_masked(oq):
 
 
 # ---- the window table ------------------------------------------------------------------------
-@pytest.mark.skipif(not os.path.isdir(REFERENCE), reason="reference sources not present")
 def test_ssim_table_equals_reference_constants(oq):
-    txt = open(os.path.join(REFERENCE, "libs", "pmbb-ivqm", "src", "xStructSimConsts.h")).read()
-    vals = np.array([float(v) for v in re.findall(r"([0-9]\.[0-9]+)f", txt)][:121], np.float32).reshape(11, 11)
+    # the reference's c_FilterF (xStructSimConsts.h:31-44), recorded by tests/golden/make_golden.py
+    doc = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "ssim_window.json")))
+    vals = np.array(doc["values"], np.float32).reshape(11, 11)
     np.testing.assert_array_equal(oq.ssim_table(0), vals)
+
+
+def test_oracle_matches_reference_build_on_example_fixture(oq):
+    """Every value the reference build gave on the example pictures (tests/golden/fencing.json)."""
+    for case in fencing_io.FIXTURE["cases"]:
+        if "mask" in case:
+            continue
+        e = case["expected"]
+        p0 = _444(fencing_io.flat(case["pic0"]), 1920, 1080)
+        p1 = _444(fencing_io.flat(case["pic1"]), 1920, 1080)
+        r = oq.frame(p0, p1, 8, True, nthreads=8)
+        assert r["gcd"] == e["gcd"] and r["sse_r2t"] == e["sse_r2t"] and r["sse_t2r"] == e["sse_t2r"]
+        np.testing.assert_allclose(r["psnr"], e["psnr"], atol=DB_TOL)
+        for k in ("ivpsnr", "ivpsnr_r2t", "ivpsnr_t2r"):
+            assert abs(r[k] - e[k]) <= DB_TOL
+        np.testing.assert_allclose(r["ssim"], e["ssim"], atol=SSIM_TOL)
+        np.testing.assert_allclose(r["msssim"], e["msssim"], atol=SSIM_TOL)
+        for k in ("ivssim", "ivssim_r2t", "ivssim_t2r"):
+            assert abs(r[k] - e[k]) <= SSIM_TOL
 
 
 # ---- closed-form expectations restated from the reference's core unit tests -------------------

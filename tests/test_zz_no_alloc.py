@@ -97,6 +97,12 @@ def test_static_psnr_rejects_what_it_cannot_hold(gpu_lib):
     r = _abi.FrameResult()
     assert lib.qmiv_psnr_static(ctypes.byref(a), ctypes.byref(a), None, ctypes.byref(r), None) == _abi.QMIV_TOO_LARGE
     assert b"8192" in lib.qmiv_last_error()
+    # a row wider than 65536 samples would overflow the kernel's 32-bit per-row difference sums
+    w, h = 65538, 2
+    d = _to_device([np.zeros((h >> s, w >> s), np.uint16) for s in (0, 1, 1)])
+    a = gpu_lib.make_pic(d, 14)
+    assert lib.qmiv_psnr_static(ctypes.byref(a), ctypes.byref(a), None, ctypes.byref(r), None) == _abi.QMIV_TOO_LARGE
+    assert b"65536" in lib.qmiv_last_error()
     ref, tst = synth.pair420(64, 32, 10, seed=5)
     host = gpu_lib.make_pic([np.ascontiguousarray(p) for p in synth.split420(ref, 64, 32)], 10)
     assert lib.qmiv_psnr_static(ctypes.byref(host), ctypes.byref(host), None, ctypes.byref(r), None) == _abi.QMIV_BAD_ARG
