@@ -121,18 +121,113 @@ def make_inputs(jobs, pinned=True):
     return host
 
 
+# ---- the reference's own CPU implementation -------------------------------------------------------
+# oracle/build_ref.sh builds the reference's metric library from its own sources for this machine
+# (x86-64-v4 on x86, the portable code paths on aarch64; on a machine without a reference checkout,
+# from the copy oracle/stage_ref.sh stages) together with oracle/ref_timing.cpp, a driver that runs
+# the application's per-frame steps with the application's processor set-up and times each step
+# (the application's own -v 3 "AvgTime" figures; the application itself only builds on x86). It is
+# run on the same synthetic pictures, written as raw .yuv files, with all host threads. The timed
+# path is what the GPU value covers: PREPROC (margin extension, interleaving), GCD, SCP and the
+# metrics; the file read is left out, as the GPU value leaves out uploads.
+REF_TIMING = os.path.join(ROOT, "oracle", "_ref", "qmiv_ref_timing")
+
+
+def _write_pair(d, w, h, seed, frames=1, drift=False, shift_seed=0):
+    from ivpsnr_gb300 import synth
+    a, b = os.path.join(d, "a_%dx%d.yuv" % (w, h)), os.path.join(d, "b_%dx%d.yuv" % (w, h))
+    with open(a, "wb") as fa, open(b, "wb") as fb:
+        for f in range(frames):
+            ref, tst = synth.pair420(w, h, BD, seed=seed + f, holes=not drift, drift=drift, shift_seed=shift_seed, frame=f)
+            fa.write(ref.astype("<u2").tobytes())
+            fb.write(tst.astype("<u2").tobytes())
+    return a, b
+
+
+def ref_cli_run(a, b, w, h, erp, sr, metrics, frames=1):
+    """The reference's processors on one pair of files: (seconds per frame on the timed path,
+    per-stage ms per frame)."""
+    cmd = [REF_TIMING, "-i0", a, "-i1", b, "-w", str(w), "-h", str(h), "-bd", str(BD), "-cf", "420", "-f", str(frames),
+           "-sr", str(sr), "-ml", ",".join(metrics), "-nth", "-1"]
+    if erp:
+        cmd.append("-erp")
+    out = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=900)
+    if out.returncode != 0:
+        raise RuntimeError("reference timing driver failed: " + out.stdout[-400:])
+    stages = json.loads(out.stdout.strip().splitlines()[-1])["avg_ms"]
+    return sum(stages.values()) * 1e-3, stages
+
+
+_REF_CLI_OK = None
+
+
+def ref_cli_ok():
+    """True when the reference's timing driver is built for this machine and runs."""
+    global _REF_CLI_OK
+    if _REF_CLI_OK is None:
+        _REF_CLI_OK = False
+        if os.path.exists(REF_TIMING):
+            import tempfile
+            try:
+                with tempfile.TemporaryDirectory() as d:
+                    a, b = _write_pair(d, 64, 32, 1)
+                    ref_cli_run(a, b, 64, 32, False, 2, ["psnr", "ivpsnr"])
+                _REF_CLI_OK = True
+            except Exception:
+                _REF_CLI_OK = False
+    return _REF_CLI_OK
+
+
+def ref_cli_sample(pairs, metrics, sr=2, frames=1, drift=False):
+    """Gpixel/s of the reference's processors over picture pairs [(w, h, erp, seed)], each written
+    to files and measured separately (one resolution per run, as the application takes it)."""
+    import tempfile
+    px, secs, stages = 0, 0.0, []
+    with tempfile.TemporaryDirectory() as d:
+        for (w, h, erp, seed) in pairs:
+            a, b = _write_pair(d, w, h, seed, frames, drift=drift, shift_seed=seed if drift else 0)
+            s, st = ref_cli_run(a, b, w, h, erp, sr, metrics, frames)
+            px += w * h
+            secs += s
+            stages.append({"picture": "%dx%d%s" % (w, h, " ERP" if erp else ""), "ms": st})
+            os.unlink(a)
+            os.unlink(b)
+    return px / secs / 1e9, secs, stages
+
+
+def host_threads():
+    return os.cpu_count() or 1
+
+
+def headline_config(jobs, in_bytes):
+    px = sum(w * h for (_, _, w, h, _) in jobs)
+    return {"workload": WORKLOAD, "pairs": len(jobs), "luma_pixels_per_step": px, "bitdepth": BD, "chroma": "4:2:0",
+            "search_range": 2, "l2": "inputs %.2f GB per step > 129 MB L2; no flush" % (in_bytes / 1e9)}
+
+
+def headline_in_bytes(jobs):
+    return sum(2 * (w * h + 2 * (w // 2) * (h // 2)) * 2 for (_, _, w, h, _) in jobs)
+
+
 def run_reference(args):
-    """CPU restatement of the reference path on all host cores (the oracle port)."""
+    """The reference's own CPU implementation of the path on all host threads: its metric library
+    built for this machine and driven as the application drives it (the oracle port where that
+    build is absent), one picture pair of the multiview workload per step, views cycled."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
     from ivpsnr_gb300 import synth
-    from oracle import oracle as oq
-    nth = os.cpu_count() or 1
+    nth = host_threads()
     jobs = jobs_list()
+    use_cli = ref_cli_ok()
+    metrics = ["psnr", "wspsnr", "ivpsnr"]
 
     def step(i):
         v, f, w, h, erp = jobs[(i * FRAMES) % len(jobs)]
+        if use_cli:
+            _, secs, _ = ref_cli_sample([(w, h, erp, synth.seed_for(1, v, f))], metrics)
+            return w * h, secs
+        from oracle import oracle as oq
         ref, tst = synth.pair420(w, h, BD, seed=synth.seed_for(1, v, f), holes=True)
         p0 = oq.upsample420(synth.split420(ref, w, h), w, h)
         p1 = oq.upsample420(synth.split420(tst, w, h), w, h)
@@ -148,33 +243,51 @@ def run_reference(args):
         px += a
         secs += b
     val = px / secs / 1e9
-    sample = "one picture pair per step (views cycled), GCD+PSNR+WS-PSNR+IV-PSNR, %d host threads" % nth
+    if use_cli:
+        kind = "reference"
+        sample = ("one picture pair per step (views cycled), the reference's metric library built from its sources "
+                  "for this host (%s), all host threads, per-frame time of PREPROC+GCD+PSNR+WS-PSNR+IV-PSNR "
+                  "(oracle/ref_timing.cpp)" % os.uname().machine)
+    else:
+        kind = "port"
+        sample = "one picture pair per step (views cycled), GCD+PSNR+WS-PSNR+IV-PSNR, oracle/ C port, %d threads" % nth
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": val, "unit": "Gpixel/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-        "config": {"workload": WORKLOAD},
-        "cpu_baseline": {"value": val, "unit": "Gpixel/s", "cores": nth, "kind": "port", "sample": sample},
+        "config": headline_config(jobs, headline_in_bytes(jobs)),
+        "cpu_baseline": {"value": val, "unit": "Gpixel/s", "cores": nth, "kind": kind, "sample": sample},
         "e2e": {"value": val, "unit": "Gpixel/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))
 
 
 def cpu_baseline_sample():
-    """Bounded CPU sample for the GPU line: two pairs (one ERP, one 1080p) on all host cores."""
+    """Bounded CPU sample for the GPU line: two pairs of the workload (one ERP 4096x2048, one
+    1920x1080) through the reference's own metric library on all host threads, and the oracle port
+    beside it."""
     from ivpsnr_gb300 import synth
     from oracle import oracle as oq
-    nth = os.cpu_count() or 1
+    nth = host_threads()
+    pairs = [(4096, 2048, True, synth.seed_for(1, 0, 0)), (1920, 1080, False, synth.seed_for(1, 3, 0))]
     px, secs = 0, 0.0
-    for (v, w, h, erp) in [(0, 4096, 2048, True), (3, 1920, 1080, False)]:
-        ref, tst = synth.pair420(w, h, BD, seed=synth.seed_for(1, v, 0), holes=True)
+    for (w, h, erp, seed) in pairs:
+        ref, tst = synth.pair420(w, h, BD, seed=seed, holes=True)
         p0 = oq.upsample420(synth.split420(ref, w, h), w, h)
         p1 = oq.upsample420(synth.split420(tst, w, h), w, h)
         t = time.perf_counter()
         oq.frame(p0, p1, BD, False, use_ws=erp, nthreads=nth)
         secs += time.perf_counter() - t
         px += w * h
-    return {"value": px / secs / 1e9, "unit": "Gpixel/s", "cores": nth, "kind": "port",
+    port = {"value": px / secs / 1e9, "unit": "Gpixel/s", "cores": nth, "kind": "port",
             "sample": "2 of 96 picture pairs (4096x2048 ERP + 1920x1080), GCD+PSNR+WS-PSNR+IV-PSNR, oracle/ C port"}
+    if not ref_cli_ok():
+        return port
+    val, rsecs, stages = ref_cli_sample(pairs, ["psnr", "wspsnr", "ivpsnr"])
+    return {"value": val, "unit": "Gpixel/s", "cores": nth, "kind": "reference",
+            "sample": "2 of 96 picture pairs (4096x2048 ERP + 1920x1080) through the reference's metric library "
+                      "built for this host (%s), all host threads, per-frame time of PREPROC+GCD+PSNR+WS-PSNR+IV-PSNR "
+                      "(oracle/ref_timing.cpp)" % os.uname().machine,
+            "seconds": rsecs, "stages_ms": stages, "port": port}
 
 
 SSIM_WORKLOAD = "ivssim-ssim-msssim-10bit-420: 17 frames 1920x1080, drifting block shifts, SR 2, REF10 window"
@@ -226,21 +339,183 @@ def ssim_workload(args, dev, stream):
     P.set_profiling(False)
     r0 = _abi.FrameResult.from_buffer_copy(bytes(res[:rsz].cpu().numpy()))
     P.close()
+    # the same batch with the full 11x11 Gaussian window (sigma 1.5) in place of the reference's 10x10
+    Pg = q.Processor(w, h, max_jobs=nf, scratch_metrics=metrics, ssim_window=q.SSIM_GAUSS11)
+    for _ in range(args.warmup):
+        Pg.calc_batch(qjobs, res.data_ptr(), sptr)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        Pg.calc_batch(qjobs, res.data_ptr(), sptr)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    g_ms = e0.elapsed_time(e1) / args.steps
+    Pg.set_profiling(True)
+    Pg.calc_batch(qjobs, res.data_ptr(), sptr)
+    g_kt = {}
+    for n, t in Pg.kernel_times():
+        g_kt[n] = g_kt.get(n, 0.0) + t
+    Pg.close()
     Pp = q.Processor(w, h, max_jobs=1, scratch_metrics=metrics)
     for (j) in qjobs[:2]:
         Pp.calc_frame(j.pic0, j.pic1, metrics, sptr)
     torch.cuda.synchronize()
-    t = time.perf_counter()
-    for j in qjobs:
-        Pp.calc_frame(j.pic0, j.pic1, metrics, sptr)
-    plain_ms = (time.perf_counter() - t) * 1e3
+    plain_ms = []
+    for _ in range(2):
+        t = time.perf_counter()
+        for j in qjobs:
+            Pp.calc_frame(j.pic0, j.pic1, metrics, sptr)
+        plain_ms.append((time.perf_counter() - t) * 1e3)
+    plain_ms = min(plain_ms)
     Pp.close()
     px = w * h * nf
-    return {"workload": SSIM_WORKLOAD, "value": px / (ms * 1e-3) / 1e9, "unit": "Gpixel/s", "ms_per_step": ms,
-            "plain_value": px / (plain_ms * 1e-3) / 1e9, "batched_over_plain": plain_ms / ms, "kernel_ms": kt,
-            # the fused kernel's window positions: every component of every frame at luma resolution
-            "quad_outputs": nf * 3 * max(0, w - 10) * max(0, h - 10),
-            "check": {"ivssim_frame0": r0.ivssim, "ssim_frame0": list(r0.ssim)[:3]}}
+    out = {"workload": SSIM_WORKLOAD, "value": px / (ms * 1e-3) / 1e9, "unit": "Gpixel/s", "ms_per_step": ms,
+           "plain_value": px / (plain_ms * 1e-3) / 1e9, "batched_over_plain": plain_ms / ms, "kernel_ms": kt,
+           "plain": "one synchronous qmiv_calc_frame per frame, wall time of the 17 calls (best of 2)",
+           "gauss11": {"window": "11x11 Gaussian sigma 1.5", "ms_per_step": g_ms, "value": px / (g_ms * 1e-3) / 1e9,
+                       "unit": "Gpixel/s", "kernel_ms": g_kt},
+           # the fused kernel's window positions: every component of every frame at luma resolution
+           "quad_outputs": nf * 3 * max(0, w - 10) * max(0, h - 10),
+           "check": {"ivssim_frame0": r0.ivssim, "ssim_frame0": list(r0.ssim)[:3]}}
+    if not args.no_cpu_baseline and ref_cli_ok():
+        val, secs, st = ref_cli_sample([(w, h, False, synth.seed_for(2, 0, 0))], ["ssim", "msssim", "ivssim"], frames=2,
+                                       drift=True)
+        out["cpu_baseline"] = {"value": val, "unit": "Gpixel/s", "cores": host_threads(), "kind": "reference",
+                               "sample": "frames 0-1 of the 17 through the reference's metric library (%s), all host "
+                                         "threads, per-frame time of PREPROC+GCD+SCP+SSIM+MS-SSIM+IV-SSIM"
+                                         % os.uname().machine,
+                               "seconds_per_frame": secs, "stages_ms": st}
+    return out
+
+
+MV_SSIM_WORKLOAD = ("multiview-all-metrics-10bit-420: 3x4096x2048 ERP + 6x1920x1080 + 3x2048x1088, 8 frames, SR 2, "
+                    "GCD + PSNR + WS-PSNR + IV-PSNR + SSIM + MS-SSIM + IV-SSIM (REF10 window)")
+
+
+def multiview_ivssim_workload(args, dev, stream, jobs, host, devbufs, planes):
+    """Every metric of the reference (IV-PSNR and IV-SSIM with PSNR, WS-PSNR, SSIM, MS-SSIM) on the
+    96-pair multiview set in one batched call per step, device-resident; the same pairs through one
+    synchronous qmiv_calc_frame each (the plain form); and end to end from pinned host memory
+    through qmiv_calc_batch_host with the results read back."""
+    import ctypes as C
+
+    import torch
+
+    import ivpsnr_gb300 as q
+    from ivpsnr_gb300 import _abi, synth
+    metrics = q.M_ALL
+    qjobs, hjobs = [], []
+    for (v, f, w, h, erp), (d0, d1), (r, t_) in zip(jobs, devbufs, host):
+        for lst, a, b in ((qjobs, d0, d1), (hjobs, r, t_)):
+            j = _abi.Job()
+            j.pic0 = q.make_pic(planes(a, w, h), BD)
+            j.pic1 = q.make_pic(planes(b, w, h), BD)
+            j.pic0.sample_bytes = j.pic1.sample_bytes = 2
+            j.metrics = metrics
+            j.use_ws = int(erp)
+            lst.append(j)
+    n = len(qjobs)
+    rsz = C.sizeof(_abi.FrameResult)
+    res = torch.zeros(n * rsz, dtype=torch.uint8, device=dev)
+    res_host = torch.zeros(n * rsz, dtype=torch.uint8, pin_memory=True)
+    P = q.Processor(4096, 2048, max_jobs=n, scratch_metrics=metrics)
+    sptr = stream.cuda_stream
+    for _ in range(args.warmup):
+        P.calc_batch(qjobs, res.data_ptr(), sptr)
+    torch.cuda.synchronize()
+    l0 = P.kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        P.calc_batch(qjobs, res.data_ptr(), sptr)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    launches = P.kernel_launches() - l0
+    P.set_profiling(True)
+    kt = {}
+    for _ in range(2):
+        P.calc_batch(qjobs, res.data_ptr(), sptr)
+        for nm, t in P.kernel_times():
+            kt[nm] = kt.get(nm, 0.0) + t / 2
+    P.set_profiling(False)
+    res_host.copy_(res)
+    torch.cuda.synchronize()
+    r0 = _abi.FrameResult.from_buffer_copy(bytes(res_host[:rsz].numpy()))
+    # end to end: pinned host pictures, grouped uploads overlapped with the measurement
+    h2d = sum(r.numel() * 2 + t_.numel() * 2 for (r, t_) in host)
+
+    def e2e_step():
+        P.calc_batch_host(hjobs, res.data_ptr(), 0, sptr)
+        res_host.copy_(res, non_blocking=True)
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    P.close()
+    # plain form: one synchronous call per pair
+    Pp = q.Processor(4096, 2048, max_jobs=1, scratch_metrics=metrics)
+    Pws = q.Processor(4096, 2048, max_jobs=1, use_ws=True, scratch_metrics=metrics)
+    plain_pics = [(j.pic0, j.pic1, erp) for j, (_, _, _, _, erp) in zip(qjobs, jobs)]
+
+    def plain_pass():
+        for p0, p1, erp in plain_pics:
+            (Pws if erp else Pp).calc_frame(p0, p1, metrics, sptr)
+    plain_pass()
+    torch.cuda.synchronize()
+    plain_ms = []
+    for _ in range(2):
+        t = time.perf_counter()
+        plain_pass()
+        torch.cuda.synchronize()
+        plain_ms.append((time.perf_counter() - t) * 1e3)
+    plain_ms = min(plain_ms)
+    Pp.close()
+    Pws.close()
+    px = sum(w * h for (_, _, w, h, _) in jobs)
+    quad_outputs = sum(3 * max(0, w - 10) * max(0, h - 10) for (_, _, w, h, _) in jobs)
+    out = {"workload": MV_SSIM_WORKLOAD, "value": px / (ms * 1e-3) / 1e9, "unit": "Gpixel/s", "ms_per_step": ms,
+           "gpu_launches": launches,
+           "plain_value": px / (plain_ms * 1e-3) / 1e9, "batched_over_plain": plain_ms / ms,
+           "plain": "one synchronous qmiv_calc_frame per pair, wall time of the 96 calls (best of 2)",
+           "e2e": {"value": px / (e2e_ms * 1e-3) / 1e9, "unit": "Gpixel/s", "ms_per_step": e2e_ms,
+                   "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": n * rsz,
+                   "call": "qmiv_calc_batch_host (pinned host pictures, grouped uploads overlapped with compute)"},
+           "kernel_ms": kt, "quad_outputs": quad_outputs,
+           "check": {"ivpsnr_pair0": r0.ivpsnr, "ivssim_pair0": r0.ivssim, "msssim_pair0": list(r0.msssim)[:3]}}
+    if not args.no_cpu_baseline and ref_cli_ok():
+        pairs = [(4096, 2048, True, synth.seed_for(1, 0, 0)), (1920, 1080, False, synth.seed_for(1, 3, 0))]
+        val, rsecs, st = ref_cli_sample(pairs, ["psnr", "wspsnr", "ivpsnr", "ssim", "msssim", "ivssim"])
+        out["cpu_baseline"] = {"value": val, "unit": "Gpixel/s", "cores": host_threads(), "kind": "reference",
+                               "sample": "2 of 96 picture pairs (4096x2048 ERP + 1920x1080) through the reference's "
+                                         "metric library (%s), all host threads, all six metrics, per-frame time "
+                                         "of the path steps" % os.uname().machine,
+                               "seconds": rsecs, "stages_ms": st}
+    return out
+
+
+def quad_roofline(line, sm_mhz):
+    """FP32 view of the fused SSIM kernel of a workload line. Per window position (one output of one
+    component) the kernel filters ten moment streams in two separable passes of 10 taps (400 flop as
+    multiply-adds), forms the stream products (about 20 flop) and evaluates four indices (about 80
+    flop): 500 flop. Counting the four indices as four separate 5-moment evaluations of 218 flop
+    each, the separable count of one SSIM index, gives 872 flop, reported as frac_per_index_count."""
+    qk = [k for k in line.get("kernel_ms", {}) if k.startswith("k_ssim_quad")]
+    if not qk or line["kernel_ms"][qk[0]] <= 0:
+        return None
+    qms = line["kernel_ms"][qk[0]]
+    fl = 500.0 * line["quad_outputs"]
+    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6
+    return {"kernel": qk[0], "bound": "fp32 pipe", "flop_per_output": 500, "outputs": line["quad_outputs"],
+            "kernel_ms": qms, "achieved_tflops": fl / (qms * 1e-3) / 1e12, "peak_tflops": fp32_peak / 1e12,
+            "frac": fl / (qms * 1e-3) / fp32_peak,
+            "frac_per_index_count": 872.0 * line["quad_outputs"] / (qms * 1e-3) / fp32_peak,
+            "peak_kind": "152 SMs x 128 FP32 lanes x 2 flop x sampled SM clock (derived, not measured)"}
 
 
 STREAM_WORKLOAD = ("erp-8k-sequence-stream: 120 frames 7680x3840 ERP 10-bit 4:2:0 from pinned host memory, "
@@ -319,11 +594,21 @@ def stream_workload(args, dev):
     P.close()
     del slots, host
     torch.cuda.empty_cache()
-    return {"workload": STREAM_WORKLOAD, "value": nf * w * h / secs / 1e9, "unit": "Gpixel/s (with uploads)",
-            "seconds": secs, "ms_per_frame": secs * 1e3 / nf, "device_ms_per_frame": dev_ms,
-            "h2d_bytes_per_frame": 2 * n * 2,
-            "check": {"ivpsnr_frame0": r0.ivpsnr, "wspsnr_frame0": list(r0.wspsnr)[:3], "ivssim_frame0": r0.ivssim,
-                      "msssim_frame0": list(r0.msssim)[:3]}}
+    out = {"workload": STREAM_WORKLOAD, "value": nf * w * h / secs / 1e9, "unit": "Gpixel/s (with uploads)",
+           "seconds": secs, "ms_per_frame": secs * 1e3 / nf, "device_ms_per_frame": dev_ms,
+           "h2d_bytes_per_frame": 2 * n * 2,
+           "check": {"ivpsnr_frame0": r0.ivpsnr, "wspsnr_frame0": list(r0.wspsnr)[:3], "ivssim_frame0": r0.ivssim,
+                     "msssim_frame0": list(r0.msssim)[:3]}}
+    if not args.no_cpu_baseline and ref_cli_ok():
+        val, rsecs, st = ref_cli_sample([(w, h, True, synth.seed_for(4, 0, 0))], ["wspsnr", "ivpsnr", "ivssim", "msssim"],
+                                        sr=4)
+        out["cpu_baseline"] = {"value": val, "unit": "Gpixel/s", "cores": host_threads(), "kind": "reference",
+                               "sample": "frame 0 of the sequence through the reference's metric library (%s), all host "
+                                         "threads, search range 4, ERP, per-frame time of "
+                                         "PREPROC+GCD+SCP+WS-PSNR+IV-PSNR+MS-SSIM+IV-SSIM (file read excluded, as "
+                                         "the device-resident time excludes uploads)" % os.uname().machine,
+                               "seconds_per_frame": rsecs, "stages_ms": st}
+    return out
 
 
 def ellipse_mask(w, h, seed):
@@ -619,12 +904,15 @@ def run_ours(args):
     in_bytes = sum(2 * (w * h + 2 * (w // 2) * (h // 2)) * 2 for (_, _, w, h, _) in jobs)
     hbm_peak, peak_kind = peaks()
     achieved = in_bytes / (cps_ms * 1e-3) / 1e9
-    traffic = None
+    # DRAM traffic and executed warp instructions per pixel of the search kernel, from one ncu
+    # capture of a smaller case of the same kernel (profiles/cps_traffic.json), scaled by pixels
+    traffic, inst_px = None, None
     tf = os.path.join(ROOT, "profiles", "cps_traffic.json")
     if os.path.exists(tf):
         try:
             d = json.load(open(tf))
             traffic = d["dram_bytes_per_pixel"] * px_per_step
+            inst_px = d.get("warp_instructions_per_pixel")
         except Exception:
             traffic = None
     # integer-pipe view: algorithmic ops per candidate (3 sub, 3 mul, 2 add/mad, 1 compare-select)
@@ -632,6 +920,8 @@ def run_ours(args):
     alg_ops = px_per_step * 2 * (25 * 9 + 10)
     sm_mhz = clk.get("sm_mhz") or 1900.0
     int_peak = 152 * 128 * sm_mhz * 1e6  # INT32 lanes x clock (derived from the sampled clock)
+    issue_peak = 152 * 4 * sm_mhz * 1e6  # warp instructions per second: 4 schedulers per SM
+    issue_frac = inst_px * px_per_step / (cps_ms * 1e-3) / issue_peak if inst_px else None
 
     # ---- the same batch captured once as a CUDA graph and replayed (qmiv_batch_graph_*) ----
     graph_line = None
@@ -704,6 +994,9 @@ def run_ours(args):
     P.close()
     Pp.close()
     Pws.close()
+    mv_ssim_line = None
+    if not args.skip_ssim and world == 1:
+        mv_ssim_line = multiview_ivssim_workload(args, dev, stream, jobs, host, devbufs, planes)
     del devbufs, host
     torch.cuda.empty_cache()
 
@@ -717,20 +1010,24 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": "Gpixel/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "pairs": len(jobs), "luma_pixels_per_step": px_per_step,
-                       "bitdepth": BD, "chroma": "4:2:0", "search_range": 2,
-                       "l2": "inputs %.2f GB per step > 129 MB L2; no flush" % (in_bytes / 1e9)},
+            "config": headline_config(jobs, in_bytes),
             "clocks": clk,
             "e2e": {"value": e2e_value, "unit": "Gpixel/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": nres * rsz, "ms_per_step": e2e_ms,
                     "call": "qmiv_calc_batch_host (pinned host pictures, grouped uploads overlapped with compute)"},
             "gpu_launches": gpu_launches,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                         "frac": achieved / hbm_peak, "traffic": traffic, "kernel": cps_name,
-                         "kernel_ms": cps_ms, "peak_kind": peak_kind},
-            "roofline_int": {"bound": "int32 issue", "achieved_tops": alg_ops / (cps_ms * 1e-3) / 1e12,
-                             "peak_tops": int_peak / 1e12, "frac": alg_ops / (cps_ms * 1e-3) / int_peak,
-                             "peak_kind": "152 SMs x 128 INT32 lanes x sampled SM clock"},
+            # the search kernel is bound by integer instruction issue: three views side by side.
+            # frac: the reference formulation's integer ops (9 per candidate) over the
+            # INT32 lane rate (above 1: the expanded-key search executes fewer instructions than that
+            # formulation counts); issue_frac: the warp instructions it does execute (ncu count per
+            # pixel) over the 4-per-cycle issue rate, i.e. the headroom left; hbm_frac: its input
+            # bytes over the measured copy bandwidth
+            "roofline": {"bound": "int32 issue", "achieved": alg_ops / (cps_ms * 1e-3) / 1e12,
+                         "peak": int_peak / 1e12, "unit": "Tops/s", "frac": alg_ops / (cps_ms * 1e-3) / int_peak,
+                         "issue_frac": issue_frac, "warp_instructions_per_pixel": inst_px,
+                         "hbm_frac": achieved / hbm_peak, "hbm_achieved_gbs": achieved, "hbm_peak_gbs": hbm_peak,
+                         "hbm_peak_kind": peak_kind, "traffic": traffic, "kernel": cps_name, "kernel_ms": cps_ms,
+                         "peak_kind": "152 SMs x 128 INT32 lanes (x4 issue slots for issue_frac) x sampled SM clock"},
             "kernel_ms": kavg,
             "plain": {"value": plain_value, "unit": "Gpixel/s", "batched_over_plain": value / world / plain_value},
             "graph": graph_line,
@@ -738,20 +1035,11 @@ def run_ours(args):
             "check": {"ivpsnr_pair0": r0.ivpsnr, "gcd_pair0": list(r0.gcd_r2t)[:3]},
         }
         if ssim_line:
-            # FP32 view of the fused SSIM kernel: per window position, two separable passes of
-            # 10 taps over 10 moment streams (400 flop), the stream products and four index
-            # evaluations, about 500 flop; peak = FP32 lanes x 2 flop x the sampled clock
-            qk = [k for k in ssim_line.get("kernel_ms", {}) if k.startswith("k_ssim_quad")]
-            if qk and ssim_line["kernel_ms"][qk[0]] > 0:
-                qms = ssim_line["kernel_ms"][qk[0]]
-                fl = 500.0 * ssim_line["quad_outputs"]
-                fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6
-                ssim_line["roofline_fp32"] = {
-                    "kernel": qk[0], "bound": "fp32 pipe", "flop_per_output": 500, "outputs": ssim_line["quad_outputs"],
-                    "kernel_ms": qms, "achieved_tflops": fl / (qms * 1e-3) / 1e12, "peak_tflops": fp32_peak / 1e12,
-                    "frac": fl / (qms * 1e-3) / fp32_peak,
-                    "peak_kind": "152 SMs x 128 FP32 lanes x 2 flop x sampled SM clock"}
+            ssim_line["roofline_fp32"] = quad_roofline(ssim_line, sm_mhz)
             line["ivssim"] = ssim_line
+        if mv_ssim_line:
+            mv_ssim_line["roofline_fp32"] = quad_roofline(mv_ssim_line, sm_mhz)
+            line["multiview_ivssim"] = mv_ssim_line
         if loss_line:
             line["loss"] = loss_line
         if stream_line:

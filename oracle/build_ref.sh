@@ -20,8 +20,12 @@ set -euo pipefail
 
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 SRC="${1:-${QMIV_REFERENCE_DIR:-/root/reference}}"
+# a machine without a reference checkout may carry the sources staged by oracle/stage_ref.sh
+if [ ! -d "$SRC/libs/pmbb-ivqm/src" ] && [ -d "$HERE/../baseline/_ref/src/libs/pmbb-ivqm/src" ]; then
+  SRC="$(cd "$HERE/../baseline/_ref/src" && pwd)"
+fi
 OUT="$HERE/_ref"
-OBJ="$OUT/obj"
+OBJ="$OUT/obj-$(uname -m)"
 
 if [ ! -d "$SRC/libs/pmbb-ivqm/src" ]; then
   echo "reference sources not found at $SRC; skipping reference build" >&2
@@ -47,6 +51,9 @@ SOURCES=()
 for f in "$SRC"/libs/pmbb-base/src/*.cpp "$SRC"/libs/pmbb-core/src/*.cpp "$SRC"/libs/pmbb-ivqm/src/*.cpp; do
   case "$(basename "$f")" in
     xIVPSNRM.cpp) continue ;;
+    # processor identification by cpuid/xgetbv: x86 only; the metric library does not use it (the
+    # command-line tool does, so on other hosts the tool does not link and qmiv_ref_timing stands in)
+    xProcInfo.cpp) if [ "$ARCH" != "x86_64" ]; then continue; fi ;;
   esac
   SOURCES+=("$f")
 done
@@ -63,27 +70,37 @@ for f in "${SOURCES[@]}"; do
     if [ "${#pids[@]}" -ge "$(nproc)" ]; then wait "${pids[0]}"; pids=("${pids[@]:1}"); fi
   fi
 done
-for p in "${pids[@]}"; do wait "$p"; done
-
-# the checker harness (this repository's code, linked against the reference objects)
-g++ "${CXXFLAGS[@]}" "$HERE/ref_harness.cpp" "${objs[@]}" -lpthread -o "$OUT/qmiv_ref_harness"
-
-# the checker of the input-side operations (colour conversion, range check / clipping)
-g++ "${CXXFLAGS[@]}" "$HERE/ref_io.cpp" "${objs[@]}" -lpthread -o "$OUT/qmiv_ref_io"
-
-# the reference's own command-line tool, to reproduce its published example values
+# the reference's own command-line tool (its published example values; the CPU baseline that
+# bench.py times), compiled alongside
 APP_OBJS=()
-for f in "$SRC/apps/QMIV/src/main_QMIV.cpp" "$SRC/apps/QMIV/src/xAppQMIV.cpp" "$SRC"/libs/pmbb-spng/src/*.cpp; do
+APP_SRCS=()
+if [ "$ARCH" = "x86_64" ]; then APP_SRCS=("$SRC/apps/QMIV/src/main_QMIV.cpp" "$SRC/apps/QMIV/src/xAppQMIV.cpp" "$SRC"/libs/pmbb-spng/src/*.cpp); fi
+for f in "${APP_SRCS[@]}"; do
   rel="${f#$SRC/}"
   o="$OBJ/$(echo "$rel" | tr '/' '_' ).o"
-  if [ ! -f "$o" ] || [ "$f" -nt "$o" ]; then g++ "${CXXFLAGS[@]}" -c "$f" -o "$o"; fi
+  if [ ! -f "$o" ] || [ "$f" -nt "$o" ]; then g++ "${CXXFLAGS[@]}" -c "$f" -o "$o" & pids+=($!); fi
   APP_OBJS+=("$o")
 done
-for f in "$SRC"/thirdparty/spng/src/spng.c "$SRC"/thirdparty/spng/src/miniz.c; do
+SPNG_SRCS=()
+if [ "$ARCH" = "x86_64" ]; then SPNG_SRCS=("$SRC"/thirdparty/spng/src/spng.c "$SRC"/thirdparty/spng/src/miniz.c); fi
+for f in "${SPNG_SRCS[@]}"; do
   o="$OBJ/$(basename "$f").o"
-  if [ ! -f "$o" ] || [ "$f" -nt "$o" ]; then gcc -O2 -w -I"$SRC/thirdparty/spng/src" -c "$f" -o "$o"; fi
+  if [ ! -f "$o" ] || [ "$f" -nt "$o" ]; then gcc -O2 -w -I"$SRC/thirdparty/spng/src" -c "$f" -o "$o" & pids+=($!); fi
   APP_OBJS+=("$o")
 done
-g++ "${APP_OBJS[@]}" "${objs[@]}" -lpthread -o "$OUT/QMIV" || echo "note: reference CLI did not link; harness is still usable" >&2
+for p in "${pids[@]}"; do wait "$p"; done
+
+# the checker harness and the checker of the input-side operations (colour conversion, range
+# check / clipping): this repository's code, linked against the reference objects
+g++ "${CXXFLAGS[@]}" "$HERE/ref_harness.cpp" "${objs[@]}" -lpthread -o "$OUT/qmiv_ref_harness" & l1=$!
+g++ "${CXXFLAGS[@]}" "$HERE/ref_io.cpp" "${objs[@]}" -lpthread -o "$OUT/qmiv_ref_io" & l2=$!
+# the timing driver of the CPU baseline (the application's per-frame steps around the library)
+g++ "${CXXFLAGS[@]}" "$HERE/ref_timing.cpp" "${objs[@]}" -lpthread -o "$OUT/qmiv_ref_timing" & l3=$!
+if [ "$ARCH" = "x86_64" ]; then
+  g++ "${APP_OBJS[@]}" "${objs[@]}" -lpthread -o "$OUT/QMIV" || echo "note: reference CLI did not link; harness is still usable" >&2
+fi
+wait $l1
+wait $l2
+wait $l3
 
 echo "reference build ready in $OUT"

@@ -183,7 +183,11 @@ def test_config3_central_differences_at_full_size(gpu_lib):
     points of a 1024x1024 picture of the batch, against the GPU gradient, 1e-4 relative. The loss
     difference is summed term by term (errors and per-position SSIM of the two evaluations
     subtracted before the picture sums), so that rounding in million-term sums does not swamp a
-    change of order 1e-10. Points where the perturbation moves an argmin are skipped."""
+    change of order 1e-10. Points where the perturbation moves an argmin are skipped. The central
+    differences still carry noise of about 3e-11 at this size (measured: repeating them with h/2
+    and h/4 moves them by that much, growing as h shrinks, so it is rounding, not truncation), so
+    the relative error is taken against max(|fd|, 10 % of the RMS gradient): at the points whose
+    derivative is far below the typical one that noise alone would exceed 1e-4 of it."""
     import torch
     n, w, h = 2, 1024, 1024
     tst, ref = _pair(n, w, h, 71)
@@ -218,6 +222,6 @@ def test_config3_central_differences_at_full_size(gpu_lib):
         fd.append(dl / (2 * hstep))
         an.append(float(g_grad[0, c, y, x]))
     fd, an = np.array(fd), np.array(an)
-    floor = 1e-2 * np.sqrt(np.mean(fd ** 2))
+    floor = 1e-1 * np.sqrt(np.mean(fd ** 2))
     rel = np.abs(an - fd) / np.maximum(np.abs(fd), floor)
-    assert rel.max() <= 1e-4, (rel.max(), np.argmax(rel))
+    assert rel.max() <= 1e-4, (rel.max(), np.argmax(rel), fd[np.argmax(rel)], an[np.argmax(rel)])
