@@ -247,39 +247,57 @@ __global__ void __launch_bounds__(kThreads, 3) k_ssim(const SsimJob* __restrict_
 // Picture 0, picture 1 and the two shift-compensated pictures share their window sums: ten
 // moment streams (S1 of the four planes; S(a^2+b^2) and S(ab) of the three pairs (P0,P1),
 // (P0,SCP1), (P1,SCP0)) give SSIM, CS, IV-SSIM T2R and R2T, against sixteen for four separate
-// pair evaluations. Tiles are 16 rows high (the ten streams' vertical sums fill shared memory
-// faster).
+// pair evaluations.
+//
+// One block of 12 warps per SM walks its tiles (24 output rows x TX columns) as a two-stage
+// pipeline with specialised warps: warps 0-5 form the vertical window sums of tile k (thread =
+// staged column x 8 output rows, so each staged sample is converted and its products formed for
+// eight outputs at once) into one of two vertical-sum buffers while warps 6-11 run the horizontal
+// pass, the four indices and the row sums of tile k-1 from the other buffer (thread = output row
+// x 7 consecutive outputs; the eight threads of a row reduce their sums by shuffles). One block
+// barrier per tile separates the two; both halves carry about the same FP32 work.
 //
 // Staging: each tile needs one box per plane (the tile's rows and columns plus the window halo,
 // its left edge rounded down to 16 bytes; half-resolution boxes for 4:2:0 chroma, which the
 // vertical pass reads at (x >> 1, y >> 1)). Boxes are raw samples in two shared-memory stages:
-// one thread issues the four bulk-tensor loads of the next tile into the other stage while the
-// block works on the current one (mbarrier per stage, every wait bounded). Planes that a tensor
-// map cannot describe (unaligned base or pitch) are staged by the block itself with plain loads
-// into the same box layout, coordinates clamped at the picture edges; the bulk loads read zeros
-// there instead. Either way those samples feed only outputs outside the valid region. The
-// vertical pass converts samples to FP32 as it reads them: 2^23 + v is formed by its bit
-// pattern and (2^23 + tc) subtracted, exactly, which centres the tile on tc, the tile-centre
-// sample of picture 1.
-constexpr int kQTY = 16, kQPairs = 5;
+// thread 0 issues the four bulk-tensor loads of tile k+2 into the stage tile k has just left
+// (mbarrier per stage, every wait bounded). Planes that a tensor map cannot describe (unaligned
+// base or pitch) are staged by the vertical warps with plain loads into the same box layout,
+// coordinates clamped at the picture edges; the bulk loads read zeros there instead. Either way
+// those samples feed only outputs outside the valid region. The vertical pass converts samples to
+// FP32 as it reads them: 2^23 + v is formed by its bit pattern and (2^23 + tc) subtracted,
+// exactly, which centres the tile on tc, the tile-centre sample of picture 1.
+constexpr int kQTY = 24, kQPairs = 5;
+constexpr int kQVR = 8;                    // output rows per vertical thread
+constexpr int kQHO = 7;                    // outputs per horizontal thread (8 per row x 7 >= TX)
+constexpr int kQVT = 64 * (kQTY / kQVR);   // vertical threads: 64 staged columns x 3 row groups
+constexpr int kQHT = 8 * kQTY;             // horizontal threads: 24 rows x 8 groups
+constexpr int kQThreads = kQVT + kQHT;
+// float2 pitch of a vertical-sum row: a horizontal warp reads 4 rows x 8 groups 7 columns apart;
+// a pitch of 8 (mod 16) float2 puts the two rows of each half-warp on disjoint bank pairs
+constexpr int kQRP = 72;
 constexpr uint32_t kQuadPolls = 1u << 22;
 template <int WIN> struct QGeo {
   static constexpr int TX = kIW - WIN + 1;
-  static constexpr int IH = kQTY + WIN - 1;
-  static constexpr int RP = WIN == 10 ? 65 : 67;                 // odd float2 pitch of the vertical sums
+  static constexpr int IH = kQTY + WIN - 1;                      // staged rows
   static constexpr int BH1 = (IH + 1) / 2 + 1;                   // box rows of a half-resolution plane
   static constexpr int SLOT = ((64 + 8) * 2 * IH + 127) / 128 * 128;  // largest box: uint16, full resolution
   static constexpr int STAGE = 4 * SLOT;
-  static constexpr int SV = kQPairs * kQTY * RP * 8;
-  static constexpr int RED = 4 * 7 * kQTY * 4;
-  static constexpr int SMEM = 2 * STAGE + SV + RED + 16;
-  static_assert(4 * 14 >= TX && 4 * 13 + 3 + WIN - 1 < RP, "tile columns");
+  static constexpr int SVB = kQPairs * kQTY * kQRP * 8;          // one vertical-sum buffer
+  static constexpr int META = 32;
+  static constexpr int SMEM = 2 * STAGE + 2 * SVB + 2 * META + 16;
+  static_assert(8 * kQHO >= TX && 7 * kQHO + kQHO - 1 + WIN - 1 < kQRP, "horizontal groups");
+  static_assert(kQTY % kQVR == 0 && kQVT % 32 == 0 && kQHT % 32 == 0 && (kQHT / 32) * 4 == kQTY, "thread roles");
+  static_assert(SMEM <= 227 * 1024, "shared memory");
 };
+// what the horizontal warps need of the tile the vertical warps staged an iteration earlier
+struct QMeta { int jb, tx, x0, y0; float tc, kcc; int pad[2]; };
 }  // namespace
 int quad_box_h(int window, int shift) { const int ih = kQTY + (window == QMIV_SSIM_GAUSS11 ? 11 : 10) - 1; return shift ? (ih + 1) / 2 + 1 : ih; }
 namespace {
 
 __device__ __forceinline__ void fence_proxy_async_shared() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void bar_vertical() { asm volatile("bar.sync 1, %0;" :: "n"(kQVT) : "memory"); }
 
 // Box origin of plane `pl` for the tile whose staged region starts at (xr, yr) = (x0-5, y0-5).
 __device__ __forceinline__ void quad_box_origin(const SsimPlane& pl, int xr, int yr, int& xs, int& ys)
@@ -290,43 +308,41 @@ __device__ __forceinline__ void quad_box_origin(const SsimPlane& pl, int xr, int
 }
 
 __device__ __forceinline__ float ssim_index(float S1a, float S1b, float Sq, float Sx, float om2c, float omc,
-                                            float k_cc, float cw0, float C1, float C2, bool calc_l)
+                                            float k_cc, float cw0, float C1, float C2)
 {
   const float sab = S1a + S1b;
   const float den_cs = fmaf(-S1b, S1b, fmaf(-S1a, S1a, Sq)) + fmaf(om2c, sab, fmaf(2.0f, k_cc, C2));
   const float cov = fmaf(-S1a, S1b, Sx) + fmaf(omc, sab, k_cc);
-  float num = fmaf(2.0f, cov, C2), den = den_cs;
-  if(calc_l)
-  { // L * CS = (nL nCS) / (dL dCS): one division (xStructSim.cpp:50-51)
-    const float mua = S1a + cw0, mub = S1b + cw0;
-    num *= fmaf(2.0f * mua, mub, C1);
-    den *= fmaf(mua, mua, fmaf(mub, mub, C1));
-  }
+  const float mua = S1a + cw0, mub = S1b + cw0;
+  // L * CS = (nL nCS) / (dL dCS): one division (xStructSim.cpp:50-51)
+  const float num = fmaf(2.0f, cov, C2) * fmaf(2.0f * mua, mub, C1);
+  const float den = den_cs * fmaf(mua, mua, fmaf(mub, mub, C1));
   return __fdividef(num, den);
 }
 
 // One plane's column pointer for the vertical pass: even/odd staged-row bases (they differ for a
-// half-resolution plane whose first staged row is odd) and the row pitch in samples.
+// half-resolution plane whose first staged row is odd) and the row pitch in samples. row0: the
+// thread's first staged row (even).
 template <typename T, int SH>
 struct QCol {
   const T* e;
   const T* o;
-  __device__ __forceinline__ QCol(const unsigned char* box, int bw, int xr, int yr, int xs, int q, int rg)
+  __device__ __forceinline__ QCol(const unsigned char* box, int bw, int xr, int yr, int xs, int q, int row0)
   {
     const T* b = reinterpret_cast<const T*>(box);
     if(SH)
     {
       const int par = yr & 1, c = ((xr + q) >> 1) - xs;
-      e = b + 2 * rg * bw + c;
+      e = b + (row0 >> 1) * bw + c;
       o = e + par * bw;
     }
     else
     {
-      e = b + 4 * rg * bw + (xr - xs) + q;
+      e = b + row0 * bw + (xr - xs) + q;
       o = e;
     }
   }
-  // staged row i (0 .. 3 + WIN - 1) of the thread's output-row group, compile-time i
+  // staged row row0 + i, compile-time i
   template <int BW>
   __device__ __forceinline__ unsigned at(int i) const
   {
@@ -335,29 +351,30 @@ struct QCol {
   }
 };
 
-// Vertical pass of a tile: thread = staged column q x output rows 4rg .. 4rg+3; five float2
-// stream pairs per output row into s_v.
+// Vertical pass of a tile: thread = staged column q x output rows kQVR*rg .. kQVR*rg+kQVR-1; five
+// float2 stream pairs per output row into the vertical-sum buffer sv ([5][kQTY][kQRP]).
 template <int WIN, typename T0, int SH0>
 __device__ __forceinline__ void quad_vpass(const unsigned char* stg, const SsimQuadJob& J, int xr, int yr, float tc,
-                                           const float2 (&gk)[WIN], float2* s_v, int q, int rg)
+                                           const float2 (&gk)[WIN], float2* sv, int q, int rg)
 {
   using G = QGeo<WIN>;
   constexpr int BW0 = quad_box_w((int)sizeof(T0), SH0), BWS = quad_box_w(2, 0);
+  const int row0 = kQVR * rg;
   int xs, ys;
   quad_box_origin(J.p0, xr, yr, xs, ys);
-  const QCol<T0, SH0> c0(stg, BW0, xr, yr, xs, q, rg);
-  const QCol<T0, SH0> c1(stg + G::SLOT, BW0, xr, yr, xs, q, rg);
+  const QCol<T0, SH0> c0(stg, BW0, xr, yr, xs, q, row0);
+  const QCol<T0, SH0> c1(stg + G::SLOT, BW0, xr, yr, xs, q, row0);
   quad_box_origin(J.scp1, xr, yr, xs, ys);
-  const QCol<uint16_t, 0> c2(stg + 2 * G::SLOT, BWS, xr, yr, xs, q, rg);
-  const QCol<uint16_t, 0> c3(stg + 3 * G::SLOT, BWS, xr, yr, xs, q, rg);
+  const QCol<uint16_t, 0> c2(stg + 2 * G::SLOT, BWS, xr, yr, xs, q, row0);
+  const QCol<uint16_t, 0> c3(stg + 3 * G::SLOT, BWS, xr, yr, xs, q, row0);
   const float2 mk = make_float2(-(8388608.0f + tc), -(8388608.0f + tc));
-  float2 acc[4][kQPairs];
+  float2 acc[kQVR][kQPairs];
   #pragma unroll
-  for(int o = 0; o < 4; o++)
+  for(int o = 0; o < kQVR; o++)
     #pragma unroll
     for(int m = 0; m < kQPairs; m++) acc[o][m] = make_float2(0.f, 0.f);
   #pragma unroll
-  for(int i = 0; i < 3 + WIN; i++)
+  for(int i = 0; i < kQVR + WIN - 1; i++)
   {
     const float2 v01 = __fadd2_rn(make_float2(__uint_as_float(0x4B000000u | c0.template at<BW0>(i)),
                                               __uint_as_float(0x4B000000u | c1.template at<BW0>(i))), mk);
@@ -372,7 +389,7 @@ __device__ __forceinline__ void quad_vpass(const unsigned char* stg, const SsimQ
     st[3] = make_float2(sq01.x + sq23.x, v01.x * v23.x);   // (P0, SCP1)
     st[4] = make_float2(sq01.y + sq23.y, v01.y * v23.y);   // (P1, SCP0)
     #pragma unroll
-    for(int o = 0; o < 4; o++)
+    for(int o = 0; o < kQVR; o++)
     {
       const int k = i - o;
       if(k < 0 || k >= WIN) continue;
@@ -381,14 +398,15 @@ __device__ __forceinline__ void quad_vpass(const unsigned char* stg, const SsimQ
     }
   }
   #pragma unroll
-  for(int o = 0; o < 4; o++)
+  for(int o = 0; o < kQVR; o++)
     #pragma unroll
-    for(int m = 0; m < kQPairs; m++) s_v[(m * kQTY + 4 * rg + o) * G::RP + q] = acc[o][m];
+    for(int m = 0; m < kQPairs; m++) sv[(m * kQTY + row0 + o) * kQRP + q] = acc[o][m];
 }
 
-// The boxes of a tile whose planes have no tensor maps, by plain loads with clamped coordinates.
+// The boxes of a tile whose planes have no tensor maps, by plain loads with clamped coordinates
+// (vertical threads tv = 0 .. kQVT-1).
 template <int WIN>
-__device__ __forceinline__ void quad_fill(unsigned char* stg, const SsimQuadJob& J, int xr, int yr)
+__device__ __forceinline__ void quad_fill(unsigned char* stg, const SsimQuadJob& J, int xr, int yr, int tv)
 {
   using G = QGeo<WIN>;
   #pragma unroll
@@ -400,7 +418,7 @@ __device__ __forceinline__ void quad_fill(unsigned char* stg, const SsimQuadJob&
     const int bw = quad_box_w(P.sbytes, P.shift), bh = P.shift ? G::BH1 : G::IH;
     const int wp = P.shift ? J.W >> 1 : J.W, hp = P.shift ? J.H >> 1 : J.H;
     unsigned char* box = stg + p * G::SLOT;
-    for(int idx = threadIdx.x; idx < bw * bh; idx += kThreads)
+    for(int idx = tv; idx < bw * bh; idx += kQVT)
     {
       const int r = idx / bw, c = idx - r * bw;
       const int64_t o = (int64_t)min(ys + r, hp - 1) * P.stride + min(xs + c, wp - 1);
@@ -410,16 +428,92 @@ __device__ __forceinline__ void quad_fill(unsigned char* stg, const SsimQuadJob&
   }
 }
 
+// Horizontal pass, indices and row sums of a tile whose vertical sums are in sv: thread = output
+// row r x outputs 7g .. 7g+6 (g = 0..7); lanes 8i .. 8i+7 of a warp hold one row.
 template <int WIN>
-__global__ void __launch_bounds__(kThreads, 3) k_ssim_quad(const SsimQuadJob* __restrict__ jobs, int njobs, int ntiles)
+__device__ __forceinline__ void quad_hpass(const SsimQuadJob& J, const QMeta& M, const float2* sv,
+                                           const float2 (&gk)[WIN], int r, int g)
+{
+  using G = QGeo<WIN>;
+  const int j0 = kQHO * g;
+  const float2* src = sv + r * kQRP + j0;
+  float2 m[kQHO][kQPairs];
+  #pragma unroll
+  for(int jj = 0; jj < kQHO; jj++)
+    #pragma unroll
+    for(int s2 = 0; s2 < kQPairs; s2++) m[jj][s2] = make_float2(0.f, 0.f);
+  #pragma unroll
+  for(int t = 0; t < kQHO + WIN - 1; t++)
+  {
+    float2 val[kQPairs];
+    #pragma unroll
+    for(int s2 = 0; s2 < kQPairs; s2++) val[s2] = src[s2 * kQTY * kQRP + t];
+    #pragma unroll
+    for(int jj = 0; jj < kQHO; jj++)
+    {
+      const int k = t - jj;
+      if(k < 0 || k >= WIN) continue;
+      #pragma unroll
+      for(int s2 = 0; s2 < kQPairs; s2++) m[jj][s2] = __ffma2_rn(gk[k], val[s2], m[jj][s2]);
+    }
+  }
+  const int wi = WIN == 11 ? 1 : 0;
+  const float cf = M.tc, k_cc = M.kcc;
+  const float cw0 = cf * c_w0[wi], om2c = c_om[wi] * 2.0f * cf, omc = c_om[wi] * cf;
+  const float C1 = J.c1, C2 = J.c2, vq0 = fmaf(2.0f, k_cc, C2);
+  const int y = M.y0 + r;
+  const int x1 = min(M.x0 + G::TX, J.W - 5), y1 = min(M.y0 + kQTY, J.H - 5);
+  const bool row_ok = y < y1;
+  const uint32_t outs = J.outs;
+  float rs[4] = { 0.f, 0.f, 0.f, 0.f };
+  #pragma unroll
+  for(int jj = 0; jj < kQHO; jj++)
+  {
+    if(!(row_ok && M.x0 + j0 + jj < x1)) continue;
+    const float S0 = m[jj][0].x, S1 = m[jj][0].y, Ss1 = m[jj][1].x, Ss0 = m[jj][1].y;
+    if(outs & 3u)
+    { // SSIM(P0, P1) and CS(P0, P1) from one reciprocal
+      const float sab = S0 + S1;
+      const float den_cs = fmaf(-S1, S1, fmaf(-S0, S0, m[jj][2].x)) + fmaf(om2c, sab, vq0);
+      const float cov = fmaf(-S0, S1, m[jj][2].y) + fmaf(omc, sab, k_cc);
+      const float num_cs = fmaf(2.0f, cov, C2);
+      const float mua = S0 + cw0, mub = S1 + cw0;
+      const float nl = fmaf(2.0f * mua, mub, C1), dl = fmaf(mua, mua, fmaf(mub, mub, C1));
+      const float rc = __fdividef(1.0f, den_cs * dl);
+      rs[0] += num_cs * nl * rc;
+      rs[1] += num_cs * dl * rc;
+    }
+    if(outs & 4u) rs[2] += ssim_index(S0, Ss1, m[jj][3].x, m[jj][3].y, om2c, omc, k_cc, cw0, C1, C2);
+    if(outs & 8u) rs[3] += ssim_index(S1, Ss0, m[jj][4].x, m[jj][4].y, om2c, omc, k_cc, cw0, C1, C2);
+  }
+  // fixed-order sum over the row's eight groups, then one store per output kind
+  #pragma unroll
+  for(int k = 0; k < 4; k++)
+  {
+    float v = rs[k];
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    v += __shfl_xor_sync(0xffffffffu, v, 2);
+    v += __shfl_xor_sync(0xffffffffu, v, 4);
+    rs[k] = v;
+  }
+  if(g == 0 && row_ok)
+  {
+    #pragma unroll
+    for(int k = 0; k < 4; k++)
+      if(outs & (1u << k)) J.partial[k][(int64_t)(y - 5) * J.tiles_x + M.tx] = rs[k];
+  }
+}
+
+template <int WIN>
+__global__ void __launch_bounds__(kQThreads, 1) k_ssim_quad(const SsimQuadJob* __restrict__ jobs, int njobs, int ntiles)
 {
   using G = QGeo<WIN>;
   extern __shared__ __align__(128) unsigned char qsm[];
-  __shared__ float s_kcc;  // (1 - W0) tc^2 W0 of the current tile, formed in FP64 by one thread
-  float2* s_v = reinterpret_cast<float2*>(qsm + 2 * G::STAGE);                 // [5][16][RP]
-  float* s_red = reinterpret_cast<float*>(qsm + 2 * G::STAGE + G::SV);          // [4][7][16]
-  uint64_t* bar = reinterpret_cast<uint64_t*>(qsm + 2 * G::STAGE + G::SV + G::RED);
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  float2* s_v = reinterpret_cast<float2*>(qsm + 2 * G::STAGE);                       // [2][5][kQTY][kQRP]
+  QMeta* meta = reinterpret_cast<QMeta*>(qsm + 2 * G::STAGE + 2 * G::SVB);           // [2]
+  uint64_t* bar = reinterpret_cast<uint64_t*>(qsm + 2 * G::STAGE + 2 * G::SVB + 2 * G::META);
+  const int tid = threadIdx.x;
+  const bool vert = tid < kQVT;
   float2 gk[WIN];
   #pragma unroll
   for(int k = 0; k < WIN; k++)
@@ -462,141 +556,98 @@ __global__ void __launch_bounds__(kThreads, 3) k_ssim_quad(const SsimQuadJob* __
     return jb;
   };
 
-  int jb = 0;
-  uint32_t phase = 0;        // bit s: parity of stage s's next completion
-  uint32_t pend = 0;         // bit s: stage s has bulk loads in flight
-  if(blockIdx.x < ntiles)
+  // Every thread keeps the same bookkeeping: pend bit s = stage s has bulk loads in flight,
+  // phase bit s = parity of stage s's next completion.
+  uint32_t pend = 0, phase = 0;
+  int jv = 0, jp = 0;  // forward-scan positions: the vertical pass's tile, the prefetched tile
+  #pragma unroll
+  for(int s = 0; s < 2; s++)
   {
-    jb = job_of(blockIdx.x, 0);
-    if(jobs[jb].tmaps) { if(tid == 0) issue(blockIdx.x, jb, 0); pend |= 1u; }
+    const int t = blockIdx.x + s * gridDim.x;
+    if(t < ntiles)
+    {
+      jp = job_of(t, jp);
+      if(jobs[jp].tmaps) { if(tid == 0) issue(t, jp, s); pend |= 1u << s; }
+    }
   }
-  int it = 0;
-  for(int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, it++)
+  for(int it = 0;; it++)
   {
+    const int tv_tile = blockIdx.x + it * gridDim.x;   // tile of the vertical pass
+    const bool do_v = tv_tile < ntiles, do_h = it >= 1 && tv_tile - (int)gridDim.x < ntiles;
+    if(!do_v && !do_h) break;
     const int stg = it & 1;
-    jb = job_of(tile, jb);
-    const SsimQuadJob& J = jobs[jb];
-    const int local = tile - J.tile_base;
-    const int ty = local / J.tiles_x, tx = local - ty * J.tiles_x;
-    const int x0 = 5 + tx * G::TX, y0 = 5 + ty * kQTY;
-    const int x1 = min(x0 + G::TX, J.W - 5), y1 = min(y0 + kQTY, J.H - 5);
-    const int xr = x0 - 5, yr = y0 - 5;
-    unsigned char* stage = qsm + stg * G::STAGE;
-
-    // the next tile's boxes go into the other stage, last read two barriers ago
-    const int nt = tile + gridDim.x;
-    if(nt < ntiles)
-    {
-      const int jn = job_of(nt, jb);
-      if(jobs[jn].tmaps) { if(tid == 0) issue(nt, jn, stg ^ 1); pend |= 1u << (stg ^ 1); }
-    }
     bool ok = true;
-    if(pend & (1u << stg))
+    if(vert)
     {
-      ok = ptx::mbar_wait_bounded(&bar[stg], (phase >> stg) & 1u, kQuadPolls);
-      phase ^= 1u << stg;
-      pend &= ~(1u << stg);
+      if(do_v)
+      {
+        jv = job_of(tv_tile, jv);
+        const SsimQuadJob& J = jobs[jv];
+        const int local = tv_tile - J.tile_base;
+        const int ty = local / J.tiles_x, tx = local - ty * J.tiles_x;
+        const int x0 = 5 + tx * G::TX, y0 = 5 + ty * kQTY;
+        const int x1 = min(x0 + G::TX, J.W - 5), y1 = min(y0 + kQTY, J.H - 5);
+        const int xr = x0 - 5, yr = y0 - 5;
+        unsigned char* stage = qsm + stg * G::STAGE;
+        if(pend & (1u << stg)) ok = ptx::mbar_wait_bounded(&bar[stg], (phase >> stg) & 1u, kQuadPolls);
+        else { quad_fill<WIN>(stage, J, xr, yr, tid); bar_vertical(); }
+        if(ok)
+        {
+          // centring offset: the tile-centre sample of picture 1, from its box
+          const int xc = min((x0 + x1) >> 1, J.W - 1), yc = min((y0 + y1) >> 1, J.H - 1);
+          int xs, ys;
+          quad_box_origin(J.p1, xr, yr, xs, ys);
+          const int bw = quad_box_w(J.p1.sbytes, J.p1.shift);
+          const int cx = (J.p1.shift ? xc >> 1 : xc) - xs, cy = (J.p1.shift ? yc >> 1 : yc) - ys;
+          const unsigned char* box = stage + G::SLOT;
+          const float tc = J.p1.sbytes == 1 ? (float)box[cy * bw + cx] : (float)reinterpret_cast<const uint16_t*>(box)[cy * bw + cx];
+          if(tid == 0)
+          {
+            QMeta mt;
+            mt.jb = jv; mt.tx = tx; mt.x0 = x0; mt.y0 = y0; mt.tc = tc;
+            mt.kcc = (float)(c_omd[wi] * (double)tc * (double)tc * c_w0d[wi]);  // one FP64 product per tile
+            mt.pad[0] = mt.pad[1] = 0;
+            meta[stg] = mt;
+          }
+          const int q = tid & 63, rg = tid >> 6;
+          float2* sv = s_v + stg * (G::SVB / 8);
+          if(J.p0.sbytes == 1)
+          {
+            if(J.p0.shift) quad_vpass<WIN, uint8_t, 1>(stage, J, xr, yr, tc, gk, sv, q, rg);
+            else           quad_vpass<WIN, uint8_t, 0>(stage, J, xr, yr, tc, gk, sv, q, rg);
+          }
+          else
+          {
+            if(J.p0.shift) quad_vpass<WIN, uint16_t, 1>(stage, J, xr, yr, tc, gk, sv, q, rg);
+            else           quad_vpass<WIN, uint16_t, 0>(stage, J, xr, yr, tc, gk, sv, q, rg);
+          }
+        }
+      }
     }
-    else quad_fill<WIN>(stage, J, xr, yr);
+    else if(do_h)
+    { // the tile the vertical warps finished in the previous iteration
+      const QMeta M = meta[stg ^ 1];
+      const int th = tid - kQVT, lane = th & 31;
+      quad_hpass<WIN>(jobs[M.jb], M, s_v + (stg ^ 1) * (G::SVB / 8), gk, 4 * (th >> 5) + (lane >> 3), lane & 7);
+    }
     if(__syncthreads_or(!ok))
-    { // a bulk load did not arrive: record it, let the other stage's load land, and stop
+    { // a bulk load did not arrive: record it, let every load in flight land, and stop
       if(tid == 0)
       {
-        if(J.status) atomicExch(J.status, (int)QMIV_DEVICE_TIMEOUT);
-        if(pend & (1u << (stg ^ 1))) ptx::mbar_wait_bounded(&bar[stg ^ 1], (phase >> (stg ^ 1)) & 1u, kQuadPolls);
+        if(jobs[jv].status) atomicExch(jobs[jv].status, (int)QMIV_DEVICE_TIMEOUT);
+        for(int s = 0; s < 2; s++)
+          if(pend & (1u << s)) ptx::mbar_wait_bounded(&bar[s], (phase >> s) & 1u, kQuadPolls);
       }
       __syncthreads();
       return;
     }
-
-    // centring offset: the tile-centre sample of picture 1, from its box
-    float tc;
+    if(do_v && (pend & (1u << stg))) { pend &= ~(1u << stg); phase ^= 1u << stg; }
+    // the stage this iteration's vertical pass read is free: tile tv_tile + 2 grid goes there
+    const int nt = tv_tile + 2 * (int)gridDim.x;
+    if(nt < ntiles)
     {
-      const int xc = min((x0 + x1) >> 1, J.W - 1), yc = min((y0 + y1) >> 1, J.H - 1);
-      int xs, ys;
-      quad_box_origin(J.p1, xr, yr, xs, ys);
-      const int bw = quad_box_w(J.p1.sbytes, J.p1.shift);
-      const int cx = (J.p1.shift ? xc >> 1 : xc) - xs, cy = (J.p1.shift ? yc >> 1 : yc) - ys;
-      const unsigned char* box = stage + G::SLOT;
-      tc = J.p1.sbytes == 1 ? (float)box[cy * bw + cx] : (float)reinterpret_cast<const uint16_t*>(box)[cy * bw + cx];
-      if(tid == 0) s_kcc = (float)(c_omd[wi] * (double)tc * (double)tc * c_w0d[wi]);
-    }
-
-    // vertical pass, specialised on the pictures' sample size and resolution
-    {
-      const int q = tid & (kIW - 1), rg = tid >> 6;
-      if(J.p0.sbytes == 1)
-      {
-        if(J.p0.shift) quad_vpass<WIN, uint8_t, 1>(stage, J, xr, yr, tc, gk, s_v, q, rg);
-        else           quad_vpass<WIN, uint8_t, 0>(stage, J, xr, yr, tc, gk, s_v, q, rg);
-      }
-      else
-      {
-        if(J.p0.shift) quad_vpass<WIN, uint16_t, 1>(stage, J, xr, yr, tc, gk, s_v, q, rg);
-        else           quad_vpass<WIN, uint16_t, 0>(stage, J, xr, yr, tc, gk, s_v, q, rg);
-      }
-    }
-    __syncthreads();
-
-    // horizontal pass and the indices: row o (lanes 0-15 / 16-31), output columns 4gi .. 4gi+3
-    if(warp < 7)
-    {
-      const int o = lane & 15, gi = 2 * warp + (lane >> 4), j0 = 4 * gi;
-      float2 m[4][kQPairs];
-      #pragma unroll
-      for(int jj = 0; jj < 4; jj++)
-        #pragma unroll
-        for(int s2 = 0; s2 < kQPairs; s2++) m[jj][s2] = make_float2(0.f, 0.f);
-      #pragma unroll
-      for(int t = 0; t < 3 + WIN; t++)
-      {
-        float2 val[kQPairs];
-        #pragma unroll
-        for(int s2 = 0; s2 < kQPairs; s2++) val[s2] = s_v[(s2 * kQTY + o) * G::RP + j0 + t];
-        #pragma unroll
-        for(int jj = 0; jj < 4; jj++)
-        {
-          const int k = t - jj;
-          if(k < 0 || k >= WIN) continue;
-          #pragma unroll
-          for(int s2 = 0; s2 < kQPairs; s2++) m[jj][s2] = __ffma2_rn(gk[k], val[s2], m[jj][s2]);
-        }
-      }
-      const float cf = tc;
-      const float k_cc = s_kcc;
-      const float cw0 = cf * c_w0[wi], om2c = c_om[wi] * 2.0f * cf, omc = c_om[wi] * cf;
-      const float C1 = J.c1, C2 = J.c2;
-      const bool row_ok = y0 + o < y1;
-      float rs[4] = { 0.f, 0.f, 0.f, 0.f };
-      #pragma unroll
-      for(int jj = 0; jj < 4; jj++)
-      {
-        if(!(row_ok && x0 + j0 + jj < x1)) continue;
-        const float S0 = m[jj][0].x, S1 = m[jj][0].y, Ss1 = m[jj][1].x, Ss0 = m[jj][1].y;
-        if(J.outs & 1u) rs[0] += ssim_index(S0, S1, m[jj][2].x, m[jj][2].y, om2c, omc, k_cc, cw0, C1, C2, true);
-        if(J.outs & 2u) rs[1] += ssim_index(S0, S1, m[jj][2].x, m[jj][2].y, om2c, omc, k_cc, cw0, C1, C2, false);
-        if(J.outs & 4u) rs[2] += ssim_index(S0, Ss1, m[jj][3].x, m[jj][3].y, om2c, omc, k_cc, cw0, C1, C2, true);
-        if(J.outs & 8u) rs[3] += ssim_index(S1, Ss0, m[jj][4].x, m[jj][4].y, om2c, omc, k_cc, cw0, C1, C2, true);
-      }
-      #pragma unroll
-      for(int k = 0; k < 4; k++)
-      {
-        const float v = rs[k] + __shfl_xor_sync(0xffffffffu, rs[k], 16);
-        if(lane < 16) s_red[(k * 7 + warp) * kQTY + o] = v;
-      }
-    }
-    __syncthreads();
-    if(tid < 4 * kQTY)
-    { // output k, row r of the tile: fixed-order sum over the 7 column warps
-      const int k = tid >> 4, r = tid & 15;
-      if(J.outs & (1u << k))
-      {
-        float s = 0.0f;
-        #pragma unroll
-        for(int w = 0; w < 7; w++) s += s_red[(k * 7 + w) * kQTY + r];
-        const int y = y0 + r;
-        if(y < y1) J.partial[k][(int64_t)(y - 5) * J.tiles_x + tx] = s;
-      }
+      jp = job_of(nt, jp);
+      if(jobs[jp].tmaps) { if(tid == 0) issue(nt, jp, stg); pend |= 1u << stg; }
     }
   }
 }
@@ -1030,19 +1081,19 @@ cudaError_t launch_ssim_quad(const SsimQuadJob* d_jobs, const SsimQuadJob* h_job
     cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dv);
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_quad<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, QGeo<10>::SMEM);
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_quad<11>, cudaFuncAttributeMaxDynamicSharedMemorySize, QGeo<11>::SMEM);
-    // three resident blocks need nearly all of the unified L1 as shared memory
+    // one resident block of ~178 KB: nearly all of the unified L1 as shared memory
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_quad<10>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_quad<11>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if(e == cudaSuccess)
-      e = wi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_ssim_quad<11>, kThreads, QGeo<11>::SMEM)
-             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_ssim_quad<10>, kThreads, QGeo<10>::SMEM);
+      e = wi ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_ssim_quad<11>, kQThreads, QGeo<11>::SMEM)
+             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_ssim_quad<10>, kQThreads, QGeo<10>::SMEM);
     if(e != cudaSuccess) return e;
     slots = std::max(1, r) * std::max(1, sms);
     resident[dv][wi].store(slots, std::memory_order_release);
   }
   const int grid = std::min(tiles, slots);
-  if(wi) k_ssim_quad<11><<<grid, kThreads, QGeo<11>::SMEM, st>>>(d_jobs, n, tiles);
-  else   k_ssim_quad<10><<<grid, kThreads, QGeo<10>::SMEM, st>>>(d_jobs, n, tiles);
+  if(wi) k_ssim_quad<11><<<grid, kQThreads, QGeo<11>::SMEM, st>>>(d_jobs, n, tiles);
+  else   k_ssim_quad<10><<<grid, kQThreads, QGeo<10>::SMEM, st>>>(d_jobs, n, tiles);
   return cudaGetLastError();
 }
 
