@@ -328,6 +328,14 @@ qmiv_status qmiv_set_cps_variant(qmiv_handle* h, int32_t v);
  * written). best_variant / best_ms (may be null) receive the choice and its CPS time. */
 qmiv_status qmiv_autotune_cps(qmiv_handle* h, const qmiv_job* jobs, int32_t n, qmiv_frame_result* results,
                               int32_t reps, qmiv_stream stream, int32_t* best_variant, double* best_ms);
+/* Test hook for the failure path of the bounded device-side waits (no counterpart in the
+ * reference). With polls > 0 the first bulk-copy wait of every block of the TMA search kernels and
+ * of the fused SSIM kernel polls, polls times, an mbarrier that no copy arrives on, gives up, and
+ * takes the failure path: the block records QMIV_DEVICE_TIMEOUT in the frame's status, waits with
+ * the full limit for its own copies in flight, and stops, so the call returns QMIV_DEVICE_TIMEOUT.
+ * 0 restores normal waits; the handle stays usable. Only calls whose pictures the bulk copies can
+ * stage (16-byte aligned device planes) reach these waits. */
+qmiv_status qmiv_test_wait_timeout(qmiv_handle* h, uint32_t polls);
 /* Per-kernel timing of the most recent calc call (CUDA events recorded on the call's
  * stream around each launch, when enabled). qmiv_kernel_times synchronises with those
  * events and returns up to max launches: names[i] (static strings) and ms[i]. */

@@ -187,6 +187,10 @@ class Processor:
         _abi.check(self.lib.qmiv_finish_sequence(self.h, ctypes.byref(r)), "qmiv_finish_sequence")
         return {n: (list(getattr(r, n)) if hasattr(getattr(r, n), "__len__") else getattr(r, n)) for n, _ in r._fields_}
 
+    def test_wait_timeout(self, polls):
+        """qmiv_test_wait_timeout: polls > 0 makes the first bulk-copy wait of every block give up."""
+        _abi.check(self.lib.qmiv_test_wait_timeout(self.h, polls), "qmiv_test_wait_timeout")
+
     def set_cps_variant(self, v):
         _abi.check(self.lib.qmiv_set_cps_variant(self.h, v), "qmiv_set_cps_variant")
 

@@ -106,6 +106,7 @@ SIGNATURES = [
     ("qmiv_cps_variant_name", ctypes.c_char_p, [c_i32]),
     ("qmiv_set_cps_variant", c_i32, [_vp, c_i32]),
     ("qmiv_autotune_cps", c_i32, [_vp, _P(Job), c_i32, _vp, c_i32, _vp, _P(c_i32), _P(c_f64)]),
+    ("qmiv_test_wait_timeout", c_i32, [_vp, c_u32]),
     ("qmiv_set_profiling", c_i32, [_vp, c_i32]),
     ("qmiv_kernel_times", c_i32, [_vp, _P(ctypes.c_char_p), _P(c_f64), c_i32]),
 ]

@@ -285,7 +285,7 @@ template <int WIN> struct QGeo {
   static constexpr int STAGE = 4 * SLOT;
   static constexpr int SVB = kQPairs * kQTY * kQRP * 8;          // one vertical-sum buffer
   static constexpr int META = 32;
-  static constexpr int SMEM = 2 * STAGE + 2 * SVB + 2 * META + 16;
+  static constexpr int SMEM = 2 * STAGE + 2 * SVB + 2 * META + 32;    // + 3 mbarriers
   static_assert(8 * kQHO >= TX && 7 * kQHO + kQHO - 1 + WIN - 1 < kQRP, "horizontal groups");
   static_assert(kQTY % kQVR == 0 && kQVT % 32 == 0 && kQHT % 32 == 0 && (kQHT / 32) * 4 == kQTY, "thread roles");
   static_assert(SMEM <= 227 * 1024, "shared memory");
@@ -505,7 +505,8 @@ __device__ __forceinline__ void quad_hpass(const SsimQuadJob& J, const QMeta& M,
 }
 
 template <int WIN>
-__global__ void __launch_bounds__(kQThreads, 1) k_ssim_quad(const SsimQuadJob* __restrict__ jobs, int njobs, int ntiles)
+__global__ void __launch_bounds__(kQThreads, 1) k_ssim_quad(const SsimQuadJob* __restrict__ jobs, int njobs, int ntiles,
+                                                             uint32_t first_wait_test_polls)
 {
   using G = QGeo<WIN>;
   extern __shared__ __align__(128) unsigned char qsm[];
@@ -526,6 +527,7 @@ __global__ void __launch_bounds__(kQThreads, 1) k_ssim_quad(const SsimQuadJob* _
   {
     ptx::mbar_init(&bar[0], 1);
     ptx::mbar_init(&bar[1], 1);
+    ptx::mbar_init(&bar[2], 1);  // no copy ever arrives on it: the target of the timeout test hook
     ptx::fence_mbar_init();
   }
   __syncthreads();
@@ -589,7 +591,9 @@ __global__ void __launch_bounds__(kQThreads, 1) k_ssim_quad(const SsimQuadJob* _
         const int x1 = min(x0 + G::TX, J.W - 5), y1 = min(y0 + kQTY, J.H - 5);
         const int xr = x0 - 5, yr = y0 - 5;
         unsigned char* stage = qsm + stg * G::STAGE;
-        if(pend & (1u << stg)) ok = ptx::mbar_wait_bounded(&bar[stg], (phase >> stg) & 1u, kQuadPolls);
+        if(pend & (1u << stg))
+          ok = (it == 0 && first_wait_test_polls) ? ptx::mbar_wait_bounded(&bar[2], 0u, first_wait_test_polls)
+                                                  : ptx::mbar_wait_bounded(&bar[stg], (phase >> stg) & 1u, kQuadPolls);
         else { quad_fill<WIN>(stage, J, xr, yr, tid); bar_vertical(); }
         if(ok)
         {
@@ -1067,7 +1071,8 @@ cudaError_t launch_ssim_bwd(const SsimBwdJob* d_jobs, const SsimBwdJob* h_jobs, 
 
 int ssim_quad_tiles_y(int H) { return H > 10 ? (H - 10 + kQTY - 1) / kQTY : 0; }
 
-cudaError_t launch_ssim_quad(const SsimQuadJob* d_jobs, const SsimQuadJob* h_jobs, int n, int window, cudaStream_t st)
+cudaError_t launch_ssim_quad(const SsimQuadJob* d_jobs, const SsimQuadJob* h_jobs, int n, int window,
+                             uint32_t first_wait_test_polls, cudaStream_t st)
 {
   int tiles = 0;
   for(int i = 0; i < n; i++) tiles = h_jobs[i].tile_base + h_jobs[i].tiles_x * h_jobs[i].tiles_y;
@@ -1092,8 +1097,8 @@ cudaError_t launch_ssim_quad(const SsimQuadJob* d_jobs, const SsimQuadJob* h_job
     resident[dv][wi].store(slots, std::memory_order_release);
   }
   const int grid = std::min(tiles, slots);
-  if(wi) k_ssim_quad<11><<<grid, kQThreads, QGeo<11>::SMEM, st>>>(d_jobs, n, tiles);
-  else   k_ssim_quad<10><<<grid, kQThreads, QGeo<10>::SMEM, st>>>(d_jobs, n, tiles);
+  if(wi) k_ssim_quad<11><<<grid, kQThreads, QGeo<11>::SMEM, st>>>(d_jobs, n, tiles, first_wait_test_polls);
+  else   k_ssim_quad<10><<<grid, kQThreads, QGeo<10>::SMEM, st>>>(d_jobs, n, tiles, first_wait_test_polls);
   return cudaGetLastError();
 }
 

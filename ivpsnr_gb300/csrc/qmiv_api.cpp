@@ -120,6 +120,7 @@ struct qmiv_handle {
   int max_w = 0, max_h = 0, max_jobs = 0;
   int device = 0, num_sms = 0;
   int cps_variant_override = -1;
+  uint32_t test_wait_polls = 0;           // qmiv_test_wait_timeout
   std::vector<Slot> slots;
   void* slot_mem = nullptr;
   void* ssim_mem = nullptr;
@@ -212,6 +213,7 @@ void derive_params(qmiv_handle* h)
   p.luma_scale = (int32_t)(w0 * m);
   p.luma_scale_log2 = pow2_log2((uint64_t)p.luma_scale);
   p.one = 1;
+  p.first_wait_test_polls = h->test_wait_polls;
 }
 
 // Does the 32-bit packed key hold for this bit depth? The 32-bit TMA search evaluates keys
@@ -875,7 +877,8 @@ qmiv_status launch_jobs(qmiv_handle* h, const LaunchPlan& P, const uint8_t* d_ta
     {
       const SsimQuadJob* d_q = reinterpret_cast<const SsimQuadJob*>(d_tab + pos);
       CUDA_TRY(prof_mark(h, h->opt.ssim_window == QMIV_SSIM_GAUSS11 ? "k_ssim_quad<11>" : "k_ssim_quad<10>", st, true));
-      CUDA_TRY(launch_ssim_quad(d_q, h->qjobs.data(), (int)h->qjobs.size(), h->opt.ssim_window, st));
+      CUDA_TRY(launch_ssim_quad(d_q, h->qjobs.data(), (int)h->qjobs.size(), h->opt.ssim_window,
+                                h->params.first_wait_test_polls, st));
       CUDA_TRY(prof_mark(h, nullptr, st, false));
       h->launches++;
     }
@@ -1156,6 +1159,14 @@ int32_t qmiv_kernel_times(qmiv_handle* h, const char** names, double* ms, int32_
     if(ms) ms[n] = t;
   }
   return n;
+}
+
+qmiv_status qmiv_test_wait_timeout(qmiv_handle* h, uint32_t polls)
+{
+  if(!h) return fail(QMIV_BAD_ARG, "handle is null");
+  h->test_wait_polls = polls;
+  h->params.first_wait_test_polls = polls;
+  return QMIV_OK;
 }
 
 qmiv_status qmiv_set_cps_variant(qmiv_handle* h, int32_t v)

@@ -61,6 +61,8 @@ struct Params {
   int32_t luma_scale;                 // s
   int32_t luma_scale_log2;            // log2(s) if s is a power of two, else -1
   uint32_t one;                       // 1, opaque to the compiler (keeps index adds on the multiply-add pipe)
+  uint32_t first_wait_test_polls;     // test hook: > 0 makes each block's first bulk-copy wait poll an idle
+                                      // barrier this many times and give up (0: normal waits)
 };
 
 // Host-side launchers (defined in the .cu files).

@@ -48,7 +48,8 @@ int ssim_quad_tiles_y(int H);
 // or half resolution, and height for the window (QMIV_SSIM_*).
 __host__ __device__ constexpr int quad_box_w(int sb, int shift) { return (shift ? 32 : 64) + 16 / sb; }
 int quad_box_h(int window, int shift);
-cudaError_t launch_ssim_quad(const SsimQuadJob* d_jobs, const SsimQuadJob* h_jobs, int n, int window, cudaStream_t st);
+cudaError_t launch_ssim_quad(const SsimQuadJob* d_jobs, const SsimQuadJob* h_jobs, int n, int window,
+                             uint32_t first_wait_test_polls, cudaStream_t st);
 
 // One DownsampleHV step of the MS-SSIM pyramid.
 struct PyrStep {
