@@ -249,10 +249,10 @@ __global__ void __launch_bounds__(kThreads, 3) k_ssim(const SsimJob* __restrict_
 // (P0,SCP1), (P1,SCP0)) give SSIM, CS, IV-SSIM T2R and R2T, against sixteen for four separate
 // pair evaluations.
 //
-// One block of 12 warps per SM walks its tiles (24 output rows x TX columns) as a two-stage
-// pipeline with specialised warps: warps 0-5 form the vertical window sums of tile k (thread =
+// One block of 16 warps per SM walks its tiles (32 output rows x TX columns) as a two-stage
+// pipeline with specialised warps: warps 0-7 form the vertical window sums of tile k (thread =
 // staged column x 8 output rows, so each staged sample is converted and its products formed for
-// eight outputs at once) into one of two vertical-sum buffers while warps 6-11 run the horizontal
+// eight outputs at once) into one of two vertical-sum buffers while warps 8-15 run the horizontal
 // pass, the four indices and the row sums of tile k-1 from the other buffer (thread = output row
 // x 7 consecutive outputs; the eight threads of a row reduce their sums by shuffles). One block
 // barrier per tile separates the two; both halves carry about the same FP32 work.
@@ -267,15 +267,16 @@ __global__ void __launch_bounds__(kThreads, 3) k_ssim(const SsimJob* __restrict_
 // those samples feed only outputs outside the valid region. The vertical pass converts samples to
 // FP32 as it reads them: 2^23 + v is formed by its bit pattern and (2^23 + tc) subtracted,
 // exactly, which centres the tile on tc, the tile-centre sample of picture 1.
-constexpr int kQTY = 24, kQPairs = 5;
+constexpr int kQTY = 32, kQPairs = 5;
 constexpr int kQVR = 8;                    // output rows per vertical thread
 constexpr int kQHO = 7;                    // outputs per horizontal thread (8 per row x 7 >= TX)
-constexpr int kQVT = 64 * (kQTY / kQVR);   // vertical threads: 64 staged columns x 3 row groups
-constexpr int kQHT = 8 * kQTY;             // horizontal threads: 24 rows x 8 groups
+constexpr int kQVT = 64 * (kQTY / kQVR);   // vertical threads: 64 staged columns x 4 row groups
+constexpr int kQHT = 8 * kQTY;             // horizontal threads: 32 rows x 8 groups
 constexpr int kQThreads = kQVT + kQHT;
-// float2 pitch of a vertical-sum row: a horizontal warp reads 4 rows x 8 groups 7 columns apart;
-// a pitch of 8 (mod 16) float2 puts the two rows of each half-warp on disjoint bank pairs
-constexpr int kQRP = 72;
+// float2 pitch of a vertical-sum row: a horizontal warp reads 4 rows x 8 groups 7 columns apart,
+// lane = 4 group + row, so each half-warp reads 4 rows x 4 groups; with a pitch of 4 (mod 16)
+// float2, row * 4 + group * 7 (mod 16) is different for all 16 lanes: no bank conflicts
+constexpr int kQRP = 68;
 constexpr uint32_t kQuadPolls = 1u << 22;
 template <int WIN> struct QGeo {
   static constexpr int TX = kIW - WIN + 1;
@@ -288,6 +289,7 @@ template <int WIN> struct QGeo {
   static constexpr int SMEM = 2 * STAGE + 2 * SVB + 2 * META + 32;    // + 3 mbarriers
   static_assert(8 * kQHO >= TX && 7 * kQHO + kQHO - 1 + WIN - 1 < kQRP, "horizontal groups");
   static_assert(kQTY % kQVR == 0 && kQVT % 32 == 0 && kQHT % 32 == 0 && (kQHT / 32) * 4 == kQTY, "thread roles");
+  static_assert(kQRP % 16 == 4, "conflict-free horizontal reads");
   static_assert(SMEM <= 227 * 1024, "shared memory");
 };
 // what the horizontal warps need of the tile the vertical warps staged an iteration earlier
@@ -429,7 +431,7 @@ __device__ __forceinline__ void quad_fill(unsigned char* stg, const SsimQuadJob&
 }
 
 // Horizontal pass, indices and row sums of a tile whose vertical sums are in sv: thread = output
-// row r x outputs 7g .. 7g+6 (g = 0..7); lanes 8i .. 8i+7 of a warp hold one row.
+// row r x outputs 7g .. 7g+6 (g = 0..7); lanes 4g + i (g = 0..7) of a warp hold its row i.
 template <int WIN>
 __device__ __forceinline__ void quad_hpass(const SsimQuadJob& J, const QMeta& M, const float2* sv,
                                            const float2 (&gk)[WIN], int r, int g)
@@ -491,9 +493,9 @@ __device__ __forceinline__ void quad_hpass(const SsimQuadJob& J, const QMeta& M,
   for(int k = 0; k < 4; k++)
   {
     float v = rs[k];
-    v += __shfl_xor_sync(0xffffffffu, v, 1);
-    v += __shfl_xor_sync(0xffffffffu, v, 2);
     v += __shfl_xor_sync(0xffffffffu, v, 4);
+    v += __shfl_xor_sync(0xffffffffu, v, 8);
+    v += __shfl_xor_sync(0xffffffffu, v, 16);
     rs[k] = v;
   }
   if(g == 0 && row_ok)
@@ -632,7 +634,7 @@ __global__ void __launch_bounds__(kQThreads, 1) k_ssim_quad(const SsimQuadJob* _
     { // the tile the vertical warps finished in the previous iteration
       const QMeta M = meta[stg ^ 1];
       const int th = tid - kQVT, lane = th & 31;
-      quad_hpass<WIN>(jobs[M.jb], M, s_v + (stg ^ 1) * (G::SVB / 8), gk, 4 * (th >> 5) + (lane >> 3), lane & 7);
+      quad_hpass<WIN>(jobs[M.jb], M, s_v + (stg ^ 1) * (G::SVB / 8), gk, 4 * (th >> 5) + (lane & 3), lane >> 2);
     }
     if(__syncthreads_or(!ok))
     { // a bulk load did not arrive: record it, let every load in flight land, and stop
@@ -1086,7 +1088,7 @@ cudaError_t launch_ssim_quad(const SsimQuadJob* d_jobs, const SsimQuadJob* h_job
     cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dv);
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_quad<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, QGeo<10>::SMEM);
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_quad<11>, cudaFuncAttributeMaxDynamicSharedMemorySize, QGeo<11>::SMEM);
-    // one resident block of ~178 KB: nearly all of the unified L1 as shared memory
+    // one resident block of ~218 KB: nearly all of the unified L1 as shared memory
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_quad<10>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_quad<11>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if(e == cudaSuccess)
