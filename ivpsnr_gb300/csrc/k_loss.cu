@@ -556,7 +556,7 @@ cudaError_t loss_backward(const LossArgs& a, const double* g_sse, const double* 
   // SSIM backward jobs, their table written on the device
   LossSsimDesc D{};
   D.ref = a.ref; D.tst = a.tst; D.scp = scp; D.g_ssim = g_ssim; D.g_tst = g_tst; D.dy = dy;
-  D.n = a.n; D.W = a.W; D.H = a.H; D.btx = ssim_bwd_tiles(a.W); D.bty = ssim_bwd_tiles(a.H);
+  D.n = a.n; D.W = a.W; D.H = a.H; D.btx = ssim_bwd_tiles(a.W); D.bty = ssim_bwd_segments(a.H);
   const int nj = a.n * 6;
   std::vector<SsimBwdJob> jobs(nj);
   for(int k = 0; k < nj; k++) jobs[k] = loss_ssim_bwd_job(D, k);

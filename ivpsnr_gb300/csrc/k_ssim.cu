@@ -777,22 +777,33 @@ __global__ void k_ssim_combine(const SsimFrame* __restrict__ frames, int nframes
 //   A_a = ds/dmu_a = CS (2 mu_b - 2 mu_a L) / D1 - 2 mu_a B - mu_b C  (and A_b symmetric),
 // the chain rule gives d SSIM / d a(q) = (1/WH) sum_p w(q-p) [A_a(p) + 2 a(q) B(p) + b(q) C(p)],
 // i.e. the coefficient maps filtered with the window and combined with the samples at q.
-// Statistics are recomputed from the pictures (nothing is stored by the forward pass). Samples
-// are centred by the tile-centre value c as in the forward kernel; the combination uses centred
-// samples with A'' = A + c (2B + C).
-constexpr int kBwdT = 32;  // output tile 32 x 32
+// Statistics are recomputed from the pictures (nothing is stored by the forward pass).
+//
+// A block walks one 32-column strip of a picture down a segment of its rows in steps of 32
+// output rows. A window at p reaches the samples [p-5, p+K1] (K1 = WIN-6), so the outputs of a
+// step need the maps of 32 + WIN - 1 position rows, of which WIN - 1 were made by the step above:
+// each step stages only its 32 new sample rows, computes window moments and maps only for its
+// 32 new position rows, and keeps from the step above the WIN - 1 last sample rows and the WIN - 1
+// last rows of the transposed horizontal pass. (A first, output-less step primes a segment.)
+// Samples are centred by the step's centre sample c; maps are formed as A'' = A + c (2B + C) so
+// that they combine with centred samples, and the kept rows of the transposed pass, which are
+// linear in the maps, move to the next step's c as A'' += (c' - c)(2B + C).
+constexpr int kBwdT = 32;          // strip width and step height
+constexpr int kBwdSegSteps = 16;   // steps per block: strips are cut into segments of 512 rows
 template <int WIN> struct BGeo {
-  static constexpr int PW = kBwdT + WIN - 1;        // window positions p whose map reaches the tile
-  static constexpr int SW = PW + WIN - 1;           // staged samples
+  static constexpr int K1 = WIN - 6;                 // a window reaches K1 samples right of / below its position
+  static constexpr int PW = kBwdT + WIN - 1;         // position columns whose maps reach the strip
+  static constexpr int SW = PW + WIN - 1;            // sample columns
+  static constexpr int KR = WIN - 1;                 // rows kept from one step to the next
+  static constexpr int SR = kBwdT + KR;              // sample rows (and transposed-pass rows) held
   // row pitches (float4) read down a column by consecutive lanes are odd: conflict-free
-  static constexpr int VP = SW | 1, MP = PW | 1;
-  // region A: staged samples [SW][SW] float2, later the coefficient maps [PW][MP] float4;
-  // region B: vertical sums [PW][VP] float4, later F [PW][33] float4; the tile's own centred
-  // samples [32][32] float2
-  static constexpr int A = (SW * SW * 8 > PW * MP * 16 ? SW * SW * 8 : PW * MP * 16);
-  static constexpr int B = PW * VP * 16;
-  static constexpr int SMEM = A + B + kBwdT * kBwdT * 8;
-  static_assert(PW * (kBwdT + 1) <= PW * VP && kBwdT * kBwdT / 4 == 256, "F aliases V; one q column x 4 rows per thread");
+  static constexpr int VP = SW | 1, MP = PW | 1, FP = kBwdT + 1;
+  static constexpr int S_SMP = SR * SW * 8;          // raw samples (a, b), float2
+  static constexpr int S_V = kBwdT * VP * 16;        // vertical moments of the step's new position rows
+  static constexpr int S_M = kBwdT * MP * 16;        // their coefficient maps
+  static constexpr int S_F = SR * FP * 16;           // transposed horizontal sums: kept rows, then new ones
+  static constexpr int SMEM = S_SMP + S_V + S_M + S_F;
+  static_assert(4 * SW <= 256 && 32 * ((PW + 7) / 8) <= 256 && KR <= kBwdT, "one round of the block per pass");
 };
 
 // acc += g * v on a float4 as two packed FP32 multiply-adds
@@ -803,20 +814,20 @@ __device__ __forceinline__ void fma4(float2 g, const float4& v, float4& acc)
   acc = make_float4(lo.x, lo.y, hi.x, hi.y);
 }
 
-// Each pass is register-blocked: a thread filters 8 consecutive outputs along the pass
-// direction from 8 + WIN - 1 shared-memory reads.
+// Each pass is register-blocked: a thread filters 8 (the last one 4) consecutive outputs along
+// the pass direction from that many + WIN - 1 shared-memory reads.
 template <int WIN>
-__global__ void __launch_bounds__(256, 3) k_ssim_bwd(const SsimBwdJob* __restrict__ jobs, int njobs)
+__global__ void __launch_bounds__(256, 2) k_ssim_bwd(const SsimBwdJob* __restrict__ jobs, int njobs)
 {
   using G = BGeo<WIN>;
-  constexpr int PW = G::PW, SW = G::SW, VP = G::VP, MP = G::MP, NG = (PW + 7) / 8;
-  static_assert(PW - 32 >= 8 && PW - 32 <= 10, "row groups");
+  constexpr int PW = G::PW, SW = G::SW, KR = G::KR, SR = G::SR, VP = G::VP, MP = G::MP, FP = G::FP, K1 = G::K1;
+  constexpr int NG = (PW + 7) / 8;
   extern __shared__ __align__(16) float smem[];
-  float2* s_in = reinterpret_cast<float2*>(smem);                    // A: [SW][SW] centred a, b
-  float4* s_m = reinterpret_cast<float4*>(smem);                     // A: [PW][MP] coefficient maps
-  float4* s_v = reinterpret_cast<float4*>(smem + G::A / 4);          // B: [PW][VP] vertical sums
-  float4* s_f = s_v;                                                 // B: [PW][33]
-  float2* s_q = reinterpret_cast<float2*>(smem + (G::A + G::B) / 4); // [32][32] centred a, b at q
+  float2* s_s = reinterpret_cast<float2*>(smem);                                      // [SR][SW]
+  float4* s_v = reinterpret_cast<float4*>(smem + G::S_SMP / 4);                       // [32][VP]
+  float4* s_m = reinterpret_cast<float4*>(smem + (G::S_SMP + G::S_V) / 4);            // [32][MP]
+  float4* s_f = reinterpret_cast<float4*>(smem + (G::S_SMP + G::S_V + G::S_M) / 4);   // [SR][FP]
+  __shared__ float s_kcc;  // (1 - W0) c^2 W0 of the step, formed in FP64 by one thread
   float2 gk[WIN];
   #pragma unroll
   for(int k = 0; k < WIN; k++) gk[k] = c_g2[k];
@@ -826,169 +837,190 @@ __global__ void __launch_bounds__(256, 3) k_ssim_bwd(const SsimBwdJob* __restric
     jb = lo; }
   const SsimBwdJob& J = jobs[jb];
   const int local = blockIdx.x - J.tile_base;
-  const int ty = local / J.tiles_x, tx = local - ty * J.tiles_x;
+  const int seg = local / J.tiles_x, strip = local - seg * J.tiles_x;
   const int W = J.W, H = J.H, tid = threadIdx.x;
-  const int qx0 = tx * kBwdT, qy0 = ty * kBwdT;
-  const int px0 = qx0 - (WIN - 6), py0 = qy0 - (WIN - 6);  // p = q - k, k in [-5, WIN-6]
-  const int sx0 = px0 - 5, sy0 = py0 - 5;
-  const float c = __ldg((const float*)J.b.ptr + (int64_t)min(qy0 + kBwdT / 2, H - 1) * J.b.stride + min(qx0 + kBwdT / 2, W - 1));
-  __shared__ float s_kcc;  // (1 - W0) c^2 W0, formed in FP64 by one thread (read after the next barrier)
-  if(tid == 0) s_kcc = (float)(c_omd[WIN == 11 ? 1 : 0] * (double)c * (double)c * c_w0d[WIN == 11 ? 1 : 0]);
+  const int qx0 = strip * kBwdT, px0 = qx0 - K1, sx0 = px0 - 5;
+  const int y_begin = seg * kBwdT * kBwdSegSteps, y_end = min(H, y_begin + kBwdT * kBwdSegSteps);
+  const int nsteps = (y_end - y_begin + kBwdT - 1) / kBwdT;
   const float* pa = (const float*)J.a.ptr;
   const float* pb = (const float*)J.b.ptr;
-  { // all loads of the tile are issued before the first store
-    constexpr int NI = (SW * SW + 255) / 256;
-    float va[NI], vb[NI];
-    #pragma unroll
-    for(int k = 0; k < NI; k++)
-    {
-      const int i = min(tid + 256 * k, SW * SW - 1);
-      const int r = i / SW, q = i - r * SW;
-      const int gx = min(max(sx0 + q, 0), W - 1), gy = min(max(sy0 + r, 0), H - 1);
-      va[k] = __ldg(pa + (int64_t)gy * J.a.stride + gx);
-      vb[k] = __ldg(pb + (int64_t)gy * J.b.stride + gx);
-    }
-    #pragma unroll
-    for(int k = 0; k < NI; k++)
-    {
-      const int i = tid + 256 * k;
-      if(i >= SW * SW) break;
-      const float2 v = make_float2(va[k] - c, vb[k] - c);
-      s_in[i] = v;
-      const int r = i / SW - (WIN - 1), q = i % SW - (WIN - 1);  // staged (WIN-1, WIN-1) is q = (0, 0)
-      if(r >= 0 && r < kBwdT && q >= 0 && q < kBwdT) s_q[r * kBwdT + q] = v;
-    }
-  }
-  __syncthreads();
-  // vertical window sums: thread = staged column q x a group of p rows (four groups of 8 and
-  // one of PW - 32), so that the SW x 5 items take one round of the 256 threads at WIN = 10
+  const int wi = WIN == 11 ? 1 : 0;
+  const float w0 = c_w0[wi], om = c_om[wi];
+  const float C1 = J.c1, C2 = J.c2;
+  const float scale = (float)(*J.g / ((double)W * (double)H));
+  float c_prev = 0.0f;
+
+  for(int st = -1; st < nsteps; st++)
   {
-    auto vpass = [&](auto nr_tag, int q, int r0) {
-      constexpr int NR = decltype(nr_tag)::value;
-      float4 acc[NR];
+    const int y = y_begin + kBwdT * st;   // output rows [y, y+32); sample row r is picture row y + r
+    const bool prime = st < 0;            // the step above the segment: makes the kept rows only
+    { // stage the new sample rows (all rows when priming), coordinates clamped; all loads first
+      const int r_lo = prime ? 0 : KR;
+      constexpr int NI = (SR * SW + 255) / 256;
+      float va[NI], vb[NI];
       #pragma unroll
-      for(int o = 0; o < NR; o++) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
-      #pragma unroll
-      for(int i = 0; i < NR + WIN - 1; i++)
+      for(int k = 0; k < NI; k++)
       {
-        const float2 ab = s_in[(r0 + i) * SW + q];
-        const float4 v = make_float4(ab.x, ab.y, fmaf(ab.x, ab.x, ab.y * ab.y), ab.x * ab.y);
+        const int i = min(r_lo * SW + tid + 256 * k, SR * SW - 1);
+        const int r = i / SW, q = i - r * SW;
+        const int gx = min(max(sx0 + q, 0), W - 1), gy = min(max(y + r, 0), H - 1);
+        va[k] = __ldg(pa + (int64_t)gy * J.a.stride + gx);
+        vb[k] = __ldg(pb + (int64_t)gy * J.b.stride + gx);
+      }
+      #pragma unroll
+      for(int k = 0; k < NI; k++)
+      {
+        const int i = r_lo * SW + tid + 256 * k;
+        if(i < SR * SW) s_s[i] = make_float2(va[k], vb[k]);
+      }
+    }
+    __syncthreads();
+    // centring: the step's centre sample of b
+    const float c = s_s[(kBwdT / 2) * SW + kBwdT / 2 + WIN - 1].y;
+    if(tid == 0) s_kcc = (float)(c_omd[wi] * (double)c * (double)c * c_w0d[wi]);
+    if(!prime)
+    { // the kept rows of the transposed pass move from the previous step's centring to this one's
+      const float d = c - c_prev;
+      for(int i = tid; i < KR * kBwdT; i += 256)
+      {
+        float4& f = s_f[(i >> 5) * FP + (i & 31)];
+        const float t = d * fmaf(2.0f, f.z, f.w);
+        f.x += t;
+        f.y += t;
+      }
+    }
+    c_prev = c;
+    // vertical moments of the new position rows j (position row y + 5 + j): thread = sample
+    // column x 8 position rows
+    for(int it = tid; it < 4 * SW; it += 256)
+    {
+      const int q = it % SW, g8 = it / SW;
+      if(prime && 8 * g8 + 7 < kBwdT - KR) continue;
+      float4 acc[8];
+      #pragma unroll
+      for(int o = 0; o < 8; o++) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+      #pragma unroll
+      for(int i = 0; i < 7 + WIN; i++)
+      {
+        const float2 ab = s_s[(8 * g8 + i) * SW + q];
+        const float a = ab.x - c, b = ab.y - c;
+        const float4 v = make_float4(a, b, fmaf(a, a, b * b), a * b);
         #pragma unroll
-        for(int o = 0; o < NR; o++)
+        for(int o = 0; o < 8; o++)
           if(i - o >= 0 && i - o < WIN) fma4(gk[i - o], v, acc[o]);
       }
       #pragma unroll
-      for(int o = 0; o < NR; o++) s_v[(r0 + o) * VP + q] = acc[o];
-    };
-    for(int it = tid; it < SW * 5; it += 256)
-    {
-      const int q = it % SW, g = it / SW;
-      if(g < 4) vpass(std::integral_constant<int, 8>{}, q, 8 * g);
-      else      vpass(std::integral_constant<int, PW - 32>{}, q, 32);
+      for(int o = 0; o < 8; o++) s_v[(8 * g8 + o) * VP + q] = acc[o];
     }
-  }
-  __syncthreads();
-  // horizontal sums -> moments at p -> coefficient maps (zero outside the valid region):
-  // thread = p row x 8 consecutive p columns
-  const int wi = WIN == 11 ? 1 : 0;
-  const float w0 = c_w0[wi], om = c_om[wi];
-  const float k_cc = s_kcc;
-  const float C1 = J.c1, C2 = J.c2;
-  for(int it = tid; it < PW * NG; it += 256)
-  {
-    const int r = it % PW, c0 = min(8 * (it / PW), PW - 8);
-    float4 acc[8];
-    #pragma unroll
-    for(int o = 0; o < 8; o++) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
-    #pragma unroll
-    for(int i = 0; i < 7 + WIN; i++)
+    __syncthreads();
+    // horizontal moments -> coefficient maps (zero outside the valid region): thread = position
+    // row x 8 consecutive position columns
     {
-      const float4 v = s_v[r * VP + c0 + i];
-      #pragma unroll
-      for(int o = 0; o < 8; o++)
-        if(i - o >= 0 && i - o < WIN) fma4(gk[i - o], v, acc[o]);
-    }
-    const int py = py0 + r;
-    const bool row_ok = py >= 5 && py < H - 5;
-    #pragma unroll
-    for(int o = 0; o < 8; o++)
-    {
-      const int px = px0 + c0 + o;
-      float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
-      if(row_ok && px >= 5 && px < W - 5)
+      const float k_cc = s_kcc;
+      for(int it = tid; it < kBwdT * NG; it += 256)
       {
-        const float4 m = acc[o];
-        const float S1a = m.x, S1b = m.y, sab = S1a + S1b;
-        const float mua = S1a + c * w0, mub = S1b + c * w0;
-        const float vsum = fmaf(-S1b, S1b, fmaf(-S1a, S1a, m.z)) + fmaf(om * 2.0f * c, sab, 2.0f * k_cc);
-        const float cov = fmaf(-S1a, S1b, m.w) + fmaf(om * c, sab, k_cc);
-        const float N1 = fmaf(2.0f * mua, mub, C1), D1 = fmaf(mua, mua, fmaf(mub, mub, C1));
-        const float N2 = fmaf(2.0f, cov, C2), D2 = vsum + C2;
-        const float r1 = __fdividef(1.0f, D1), r2 = __fdividef(1.0f, D2);  // D1 >= C1, D2 ~ >= C2: far from 0
-        const float L = N1 * r1, CS = N2 * r2;
-        const float B = -L * CS * r2, Cc = 2.0f * L * r2;
-        const float Aa = CS * (2.0f * mub - 2.0f * mua * L) * r1 - 2.0f * mua * B - mub * Cc;
-        const float Ab = CS * (2.0f * mua - 2.0f * mub * L) * r1 - 2.0f * mub * B - mua * Cc;
-        const float cc = c * (2.0f * B + Cc);
-        out = make_float4(Aa + cc, Ab + cc, B, Cc);
-      }
-      s_m[r * MP + c0 + o] = out;
-    }
-  }
-  __syncthreads();
-  // transposed horizontal pass: F[pr][qc] = sum_j g[j] M[pr][qc + WIN-1-j];
-  // thread = p row x 8 consecutive q columns (F reuses the V area, pitch FP float4)
-  constexpr int FP = kBwdT + 1;
-  for(int it = tid; it < PW * (kBwdT / 8); it += 256)
-  {
-    const int r = it % PW, q0 = 8 * (it / PW);
-    float4 acc[8];
-    #pragma unroll
-    for(int o = 0; o < 8; o++) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
-    #pragma unroll
-    for(int i = 0; i < 7 + WIN; i++)
-    {
-      const float4 v = s_m[r * MP + q0 + i];
-      #pragma unroll
-      for(int o = 0; o < 8; o++)
-        if(o + WIN - 1 - i >= 0 && o + WIN - 1 - i < WIN) fma4(gk[o + WIN - 1 - i], v, acc[o]);
-    }
-    #pragma unroll
-    for(int o = 0; o < 8; o++) s_f[r * FP + q0 + o] = acc[o];
-  }
-  __syncthreads();
-  // transposed vertical pass and the combination: thread = q column x 4 consecutive q rows, so
-  // that all 256 threads work and a warp's stores cover consecutive columns of a row
-  const float scale = (float)(*J.g / ((double)W * (double)H));
-  {
-    const int cq = tid % kBwdT, q0 = 4 * (tid / kBwdT);
-    const int x = qx0 + cq;
-    float4 acc[4];
-    #pragma unroll
-    for(int o = 0; o < 4; o++) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
-    #pragma unroll
-    for(int i = 0; i < 3 + WIN; i++)
-    {
-      const float4 v = s_f[(q0 + i) * FP + cq];
-      #pragma unroll
-      for(int o = 0; o < 4; o++)
-        if(o + WIN - 1 - i >= 0 && o + WIN - 1 - i < WIN) fma4(gk[o + WIN - 1 - i], v, acc[o]);
-    }
-    if(x < W)
-    {
-      #pragma unroll
-      for(int o = 0; o < 4; o++)
-      {
-        const int y = qy0 + q0 + o;
-        if(y >= H) break;
-        const float4 f = acc[o];
-        const float2 v = s_q[(q0 + o) * kBwdT + cq];  // the centred samples at q
-        if(J.outx) J.outx[(int64_t)y * W + x] = scale * (f.x + 2.0f * v.x * f.z + v.y * f.w);
-        if(J.outy) J.outy[(int64_t)y * W + x] = scale * (f.y + 2.0f * v.y * f.z + v.x * f.w);
+        const int r = it % kBwdT, c0 = min(8 * (it / kBwdT), PW - 8);
+        if(prime && r < kBwdT - KR) continue;
+        float4 acc[8];
+        #pragma unroll
+        for(int o = 0; o < 8; o++) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+        #pragma unroll
+        for(int i = 0; i < 7 + WIN; i++)
+        {
+          const float4 v = s_v[r * VP + c0 + i];
+          #pragma unroll
+          for(int o = 0; o < 8; o++)
+            if(i - o >= 0 && i - o < WIN) fma4(gk[i - o], v, acc[o]);
+        }
+        const int py = y + 5 + r;
+        const bool row_ok = py >= 5 && py < H - 5;
+        #pragma unroll
+        for(int o = 0; o < 8; o++)
+        {
+          const int px = px0 + c0 + o;
+          float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+          if(row_ok && px >= 5 && px < W - 5)
+          {
+            const float4 m = acc[o];
+            const float S1a = m.x, S1b = m.y, sab = S1a + S1b;
+            const float mua = S1a + c * w0, mub = S1b + c * w0;
+            const float vsum = fmaf(-S1b, S1b, fmaf(-S1a, S1a, m.z)) + fmaf(om * 2.0f * c, sab, 2.0f * k_cc);
+            const float cov = fmaf(-S1a, S1b, m.w) + fmaf(om * c, sab, k_cc);
+            const float N1 = fmaf(2.0f * mua, mub, C1), D1 = fmaf(mua, mua, fmaf(mub, mub, C1));
+            const float N2 = fmaf(2.0f, cov, C2), D2 = vsum + C2;
+            const float r1 = __fdividef(1.0f, D1), r2 = __fdividef(1.0f, D2);  // D1 >= C1, D2 ~ >= C2: far from 0
+            const float L = N1 * r1, CS = N2 * r2;
+            const float B = -L * CS * r2, Cc = 2.0f * L * r2;
+            const float Aa = CS * (2.0f * mub - 2.0f * mua * L) * r1 - 2.0f * mua * B - mub * Cc;
+            const float Ab = CS * (2.0f * mua - 2.0f * mub * L) * r1 - 2.0f * mub * B - mua * Cc;
+            const float cc = c * (2.0f * B + Cc);
+            out = make_float4(Aa + cc, Ab + cc, B, Cc);
+          }
+          s_m[r * MP + c0 + o] = out;
+        }
       }
     }
+    __syncthreads();
+    // transposed horizontal pass of the new rows: F[KR + r][qc] = sum_j g[j] M[r][qc + WIN-1-j];
+    // thread = position row x 8 consecutive output columns
+    for(int it = tid; it < kBwdT * (kBwdT / 8); it += 256)
+    {
+      const int r = it % kBwdT, q0 = 8 * (it / kBwdT);
+      if(prime && r < kBwdT - KR) continue;
+      float4 acc[8];
+      #pragma unroll
+      for(int o = 0; o < 8; o++) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+      #pragma unroll
+      for(int i = 0; i < 7 + WIN; i++)
+      {
+        const float4 v = s_m[r * MP + q0 + i];
+        #pragma unroll
+        for(int o = 0; o < 8; o++)
+          if(o + WIN - 1 - i >= 0 && o + WIN - 1 - i < WIN) fma4(gk[o + WIN - 1 - i], v, acc[o]);
+      }
+      #pragma unroll
+      for(int o = 0; o < 8; o++) s_f[(KR + r) * FP + q0 + o] = acc[o];
+    }
+    __syncthreads();
+    if(!prime)
+    { // transposed vertical pass and the combination: thread = output column x 4 consecutive
+      // output rows (transposed-pass row f is position row y - K1 + f)
+      const int cq = tid % kBwdT, q0 = 4 * (tid / kBwdT);
+      const int x = qx0 + cq;
+      float4 acc[4];
+      #pragma unroll
+      for(int o = 0; o < 4; o++) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+      #pragma unroll
+      for(int i = 0; i < 3 + WIN; i++)
+      {
+        const float4 v = s_f[(q0 + i) * FP + cq];
+        #pragma unroll
+        for(int o = 0; o < 4; o++)
+          if(o + WIN - 1 - i >= 0 && o + WIN - 1 - i < WIN) fma4(gk[o + WIN - 1 - i], v, acc[o]);
+      }
+      if(x < W)
+      {
+        #pragma unroll
+        for(int o = 0; o < 4; o++)
+        {
+          const int yy = y + q0 + o;
+          if(yy >= y_end) break;
+          const float4 f = acc[o];
+          const float2 s = s_s[(q0 + o) * SW + cq + WIN - 1];  // the samples at q
+          const float a = s.x - c, b = s.y - c;
+          if(J.outx) J.outx[(int64_t)yy * W + x] = scale * (f.x + 2.0f * a * f.z + b * f.w);
+          if(J.outy) J.outy[(int64_t)yy * W + x] = scale * (f.y + 2.0f * b * f.z + a * f.w);
+        }
+      }
+    }
+    __syncthreads();
+    // keep the last WIN - 1 sample rows and transposed-pass rows for the next step
+    for(int i = tid; i < KR * SW; i += 256) s_s[i] = s_s[kBwdT * SW + i];
+    for(int i = tid; i < KR * kBwdT; i += 256) s_f[(i >> 5) * FP + (i & 31)] = s_f[(kBwdT + (i >> 5)) * FP + (i & 31)];
+    __syncthreads();
   }
 }
+
 
 }  // namespace
 
@@ -1048,6 +1080,7 @@ cudaError_t launch_ssim(const SsimJob* d_jobs, const SsimJob* h_jobs, int n, int
 }
 
 int ssim_bwd_tiles(int dim) { return (dim + kBwdT - 1) / kBwdT; }
+int ssim_bwd_segments(int H) { return (H + kBwdT * kBwdSegSteps - 1) / (kBwdT * kBwdSegSteps); }
 
 cudaError_t launch_ssim_bwd(const SsimBwdJob* d_jobs, const SsimBwdJob* h_jobs, int n, int window, cudaStream_t st)
 {
@@ -1060,7 +1093,7 @@ cudaError_t launch_ssim_bwd(const SsimBwdJob* d_jobs, const SsimBwdJob* h_jobs, 
   {
     cudaError_t e = cudaFuncSetAttribute(k_ssim_bwd<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, BGeo<10>::SMEM);
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_bwd<11>, cudaFuncAttributeMaxDynamicSharedMemorySize, BGeo<11>::SMEM);
-    // three resident blocks of 68-72 KB need the unified L1 mostly as shared memory
+    // two resident blocks of 83-87 KB need the unified L1 mostly as shared memory
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_bwd<10>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_bwd<11>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if(e != cudaSuccess) return e;

@@ -81,7 +81,8 @@ struct SsimBwdJob {
   float* outx;           // d/da, W x H with row pitch W (null: not needed)
   float* outy;           // d/db (null: not needed)
 };
-int ssim_bwd_tiles(int dim);
+int ssim_bwd_tiles(int dim);        // 32-column strips of a row of width dim
+int ssim_bwd_segments(int H);       // row segments a strip is cut into
 cudaError_t launch_ssim_bwd(const SsimBwdJob* d_jobs, const SsimBwdJob* h_jobs, int n, int window, cudaStream_t st);
 
 cudaError_t ssim_set_window_constants(const float g[11], const double w0[2]);
