@@ -799,11 +799,12 @@ template <int WIN> struct BGeo {
   // row pitches (float4) read down a column by consecutive lanes are odd: conflict-free
   static constexpr int VP = SW | 1, MP = PW | 1, FP = kBwdT + 1;
   static constexpr int S_SMP = SR * SW * 8;          // raw samples (a, b), float2
-  static constexpr int S_V = kBwdT * VP * 16;        // vertical moments of the step's new position rows
-  static constexpr int S_M = kBwdT * MP * 16;        // their coefficient maps
-  static constexpr int S_F = SR * FP * 16;           // transposed horizontal sums: kept rows, then new ones
-  static constexpr int SMEM = S_SMP + S_V + S_M + S_F;
-  static_assert(4 * SW <= 256 && 32 * ((PW + 7) / 8) <= 256 && KR <= kBwdT, "one round of the block per pass");
+  static constexpr int S_K = KR * FP * 16;           // transposed horizontal sums kept from the step above
+  static constexpr int S_V = kBwdT * VP * 16;        // vertical moments of the step's new position rows; once
+                                                     // they are consumed, the new transposed sums (pitch FP)
+  static constexpr int S_M = kBwdT * MP * 16;        // coefficient maps of the new position rows
+  static constexpr int SMEM = S_SMP + S_K + S_V + S_M;
+  static_assert(4 * SW <= 256 && 32 * ((PW + 7) / 8) <= 256 && KR <= kBwdT && FP <= VP, "one round of the block per pass");
 };
 
 // acc += g * v on a float4 as two packed FP32 multiply-adds
@@ -817,16 +818,18 @@ __device__ __forceinline__ void fma4(float2 g, const float4& v, float4& acc)
 // Each pass is register-blocked: a thread filters 8 (the last one 4) consecutive outputs along
 // the pass direction from that many + WIN - 1 shared-memory reads.
 template <int WIN>
-__global__ void __launch_bounds__(256, 2) k_ssim_bwd(const SsimBwdJob* __restrict__ jobs, int njobs)
+__global__ void __launch_bounds__(256, 3) k_ssim_bwd(const SsimBwdJob* __restrict__ jobs, int njobs)
 {
   using G = BGeo<WIN>;
   constexpr int PW = G::PW, SW = G::SW, KR = G::KR, SR = G::SR, VP = G::VP, MP = G::MP, FP = G::FP, K1 = G::K1;
   constexpr int NG = (PW + 7) / 8;
   extern __shared__ __align__(16) float smem[];
   float2* s_s = reinterpret_cast<float2*>(smem);                                      // [SR][SW]
-  float4* s_v = reinterpret_cast<float4*>(smem + G::S_SMP / 4);                       // [32][VP]
-  float4* s_m = reinterpret_cast<float4*>(smem + (G::S_SMP + G::S_V) / 4);            // [32][MP]
-  float4* s_f = reinterpret_cast<float4*>(smem + (G::S_SMP + G::S_V + G::S_M) / 4);   // [SR][FP]
+  // transposed horizontal sums [SR][FP]: the KR kept rows directly before the vertical-moment
+  // buffer [32][VP], whose space the 32 new rows take once the moments are consumed
+  float4* s_f = reinterpret_cast<float4*>(smem + G::S_SMP / 4);
+  float4* s_v = reinterpret_cast<float4*>(smem + (G::S_SMP + G::S_K) / 4);
+  float4* s_m = reinterpret_cast<float4*>(smem + (G::S_SMP + G::S_K + G::S_V) / 4);   // [32][MP]
   __shared__ float s_kcc;  // (1 - W0) c^2 W0 of the step, formed in FP64 by one thread
   float2 gk[WIN];
   #pragma unroll
@@ -962,24 +965,25 @@ __global__ void __launch_bounds__(256, 2) k_ssim_bwd(const SsimBwdJob* __restric
     }
     __syncthreads();
     // transposed horizontal pass of the new rows: F[KR + r][qc] = sum_j g[j] M[r][qc + WIN-1-j];
-    // thread = position row x 8 consecutive output columns
-    for(int it = tid; it < kBwdT * (kBwdT / 8); it += 256)
+    // thread = position row x 4 consecutive output columns (all 256 threads)
     {
-      const int r = it % kBwdT, q0 = 8 * (it / kBwdT);
-      if(prime && r < kBwdT - KR) continue;
-      float4 acc[8];
-      #pragma unroll
-      for(int o = 0; o < 8; o++) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
-      #pragma unroll
-      for(int i = 0; i < 7 + WIN; i++)
+      const int r = tid % kBwdT, q0 = 4 * (tid / kBwdT);
+      if(!(prime && r < kBwdT - KR))
       {
-        const float4 v = s_m[r * MP + q0 + i];
+        float4 acc[4];
         #pragma unroll
-        for(int o = 0; o < 8; o++)
-          if(o + WIN - 1 - i >= 0 && o + WIN - 1 - i < WIN) fma4(gk[o + WIN - 1 - i], v, acc[o]);
+        for(int o = 0; o < 4; o++) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+        #pragma unroll
+        for(int i = 0; i < 3 + WIN; i++)
+        {
+          const float4 v = s_m[r * MP + q0 + i];
+          #pragma unroll
+          for(int o = 0; o < 4; o++)
+            if(o + WIN - 1 - i >= 0 && o + WIN - 1 - i < WIN) fma4(gk[o + WIN - 1 - i], v, acc[o]);
+        }
+        #pragma unroll
+        for(int o = 0; o < 4; o++) s_f[(KR + r) * FP + q0 + o] = acc[o];
       }
-      #pragma unroll
-      for(int o = 0; o < 8; o++) s_f[(KR + r) * FP + q0 + o] = acc[o];
     }
     __syncthreads();
     if(!prime)
@@ -1093,7 +1097,7 @@ cudaError_t launch_ssim_bwd(const SsimBwdJob* d_jobs, const SsimBwdJob* h_jobs, 
   {
     cudaError_t e = cudaFuncSetAttribute(k_ssim_bwd<10>, cudaFuncAttributeMaxDynamicSharedMemorySize, BGeo<10>::SMEM);
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_bwd<11>, cudaFuncAttributeMaxDynamicSharedMemorySize, BGeo<11>::SMEM);
-    // two resident blocks of 83-87 KB need the unified L1 mostly as shared memory
+    // three resident blocks of 67-70 KB need the unified L1 mostly as shared memory
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_bwd<10>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if(e == cudaSuccess) e = cudaFuncSetAttribute(k_ssim_bwd<11>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if(e != cudaSuccess) return e;
