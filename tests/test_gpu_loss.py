@@ -52,12 +52,16 @@ CASES = [(2, 160, 128, 11, {}), (1, 96, 80, 12, {"search_range": 1}), (1, 128, 6
          (1, 64, 48, 14, {"search_range": 3, "unnoticeable": (0.001, 0.03, 0.03)}),
          # ragged tiles: 100x70 (partial 32x16 tiles, plane a multiple of 4) at the largest range,
          # 99x37 (plane not a multiple of 4: the scalar reduction path)
-         (1, 100, 70, 15, {"search_range": 4}), (2, 99, 37, 16, {})]
+         (1, 100, 70, 15, {"search_range": 4}), (2, 99, 37, 16, {}),
+         # weights other than (4, 1, 1): the search's general form (the default weights take a form
+         # with the luma doubled in place of the weight products)
+         (1, 96, 64, 17, {"cmp_w_search": (3, 2, 1)})]
 
 
 def _kw(opts):
     return {"sr": opts.get("search_range", 2), "unc": opts.get("unnoticeable", (0.01, 0.01, 0.01)),
-            "win": 11 if opts.get("ssim_window", 0) == 1 else 10}
+            "win": 11 if opts.get("ssim_window", 0) == 1 else 10,
+            "w_search": tuple(float(v) for v in opts.get("cmp_w_search", (4, 1, 1)))}
 
 
 @pytest.mark.parametrize("n,w,h,seed,opts", CASES)
