@@ -86,12 +86,7 @@ __global__ void k_loss_gcd_final(Geo g, const double* __restrict__ part, float u
 }
 
 // ---- corresponding-pixel search, both directions ----------------------------------------------
-// W411: the weights are (4, 1, 1). The luma samples (and the luma GCD) are then staged doubled:
-// every luma difference is doubled exactly, its square is 4 d^2 exactly (scaling by powers of two
-// commutes with rounding), and the products by 1 are exact, so the error of a candidate equals
-// ((4 d0^2) + d1^2) + d2^2 bit for bit without the three weight products; the argmin's errors
-// and shift-compensated samples are halved back, exactly.
-template <int SR, bool W411>
+template <int SR>
 __global__ void __launch_bounds__(kCpsTX * kCpsTY) k_loss_cps(Geo g, float w0, float w1, float w2,
                                                               const float* __restrict__ gcd, uint16_t* __restrict__ maps,
                                                               float* __restrict__ scp, double* __restrict__ sse_part,
@@ -117,7 +112,6 @@ __global__ void __launch_bounds__(kCpsTX * kCpsTY) k_loss_cps(Geo g, float w0, f
       const int64_t o = (int64_t)c * g.plane + (int64_t)gy * g.W + gx;
       vt[k] = __ldg(T + o);
       vr[k] = __ldg(R + o);
-      if(W411 && c == 0) { vt[k] *= 2.0f; vr[k] *= 2.0f; }
     }
     #pragma unroll
     for(int k = 0; k < NI; k++)
@@ -140,7 +134,6 @@ __global__ void __launch_bounds__(kCpsTX * kCpsTY) k_loss_cps(Geo g, float w0, f
     for(int c = 0; c < 3; c++)
     {
       gc[c] = gcd[b * 3 + c];
-      if(W411 && c == 0) gc[c] *= 2.0f;
       tg[c] = __fadd_rn(s_rt[c][ly + SR][lx + SR].y, gc[c]);
       rg[c] = __fsub_rn(s_rt[c][ly + SR][lx + SR].x, gc[c]);
     }
@@ -163,9 +156,8 @@ __global__ void __launch_bounds__(kCpsTX * kCpsTY) k_loss_cps(Geo g, float w0, f
         const float2 d0 = __fadd2_rn(s_rt[0][cy][cx], ntg[0]);
         const float2 d1 = __fadd2_rn(s_rt[1][cy][cx], ntg[1]);
         const float2 d2 = __fadd2_rn(s_rt[2][cy][cx], ntg[2]);
-        const float2 E = W411 ? __fadd2_rn(__fadd2_rn(__fmul2_rn(d0, d0), __fmul2_rn(d1, d1)), __fmul2_rn(d2, d2))
-                              : __fadd2_rn(__fadd2_rn(__fmul2_rn(wp0, __fmul2_rn(d0, d0)), __fmul2_rn(wp1, __fmul2_rn(d1, d1))),
-                                           __fmul2_rn(wp2, __fmul2_rn(d2, d2)));
+        const float2 E = __fadd2_rn(__fadd2_rn(__fmul2_rn(wp0, __fmul2_rn(d0, d0)), __fmul2_rn(wp1, __fmul2_rn(d1, d1))),
+                                    __fmul2_rn(wp2, __fmul2_rn(d2, d2)));
         const float E1 = E.x, E0 = E.y;
         const int k = dy * (2 * SR + 1) + dx;
         if(E1 < best1) { best1 = E1; k1 = k; }
@@ -183,10 +175,9 @@ __global__ void __launch_bounds__(kCpsTX * kCpsTY) k_loss_cps(Geo g, float w0, f
     for(int c = 0; c < 3; c++)
     {
       const float rv = s_rt[c][c1y][c1x].x, tv = s_rt[c][c0y][c0x].y;
-      const float h = (W411 && c == 0) ? 0.5f : 1.0f;  // undoes the doubled luma, exactly
-      e1[c] = __fsub_rn(tg[c], rv) * h;
-      e0[c] = __fsub_rn(rg[c], tv) * h;
-      const float a1 = __fsub_rn(rv, gc[c]) * h, a0 = __fadd_rn(tv, gc[c]) * h;
+      e1[c] = __fsub_rn(tg[c], rv);
+      e0[c] = __fsub_rn(rg[c], tv);
+      const float a1 = __fsub_rn(rv, gc[c]), a0 = __fadd_rn(tv, gc[c]);
       if(a1 >= 0.f && a1 <= 1.f) m1 |= 256 << c;
       if(a0 >= 0.f && a0 <= 1.f) m0 |= 256 << c;
       scp1[(int64_t)c * g.plane + pix] = fminf(fmaxf(a1, 0.f), 1.f);
@@ -532,19 +523,13 @@ cudaError_t loss_forward(const LossArgs& a, double* sse, double* ssim, cudaStrea
   k_loss_gcd_part<<<dim3(kLossGcdChunks, a.n * 3), 256, 0, st>>>(g, gpart);
   k_loss_gcd_final<<<(a.n * 3 + 63) / 64, 64, 0, st>>>(g, gpart, a.unc[0], a.unc[1], a.unc[2], gcd, ok);
   const dim3 grid(L.cps_blocks, a.n);
-  const bool w411 = a.w_search[0] == 4.0f && a.w_search[1] == 1.0f && a.w_search[2] == 1.0f;
-#define QMIV_LOSS_CPS(SRV) (w411 ? k_loss_cps<SRV, true><<<grid, kCpsTX * kCpsTY, 0, st>>>(g, a.w_search[0], a.w_search[1], \
-                                     a.w_search[2], gcd, maps, scp, ssep, L.cps_blocks) \
-                               : k_loss_cps<SRV, false><<<grid, kCpsTX * kCpsTY, 0, st>>>(g, a.w_search[0], a.w_search[1], \
-                                     a.w_search[2], gcd, maps, scp, ssep, L.cps_blocks))
   switch(a.sr)
   {
-    case 1: QMIV_LOSS_CPS(1); break;
-    case 2: QMIV_LOSS_CPS(2); break;
-    case 3: QMIV_LOSS_CPS(3); break;
-    default: QMIV_LOSS_CPS(4); break;
+    case 1: k_loss_cps<1><<<grid, kCpsTX * kCpsTY, 0, st>>>(g, a.w_search[0], a.w_search[1], a.w_search[2], gcd, maps, scp, ssep, L.cps_blocks); break;
+    case 2: k_loss_cps<2><<<grid, kCpsTX * kCpsTY, 0, st>>>(g, a.w_search[0], a.w_search[1], a.w_search[2], gcd, maps, scp, ssep, L.cps_blocks); break;
+    case 3: k_loss_cps<3><<<grid, kCpsTX * kCpsTY, 0, st>>>(g, a.w_search[0], a.w_search[1], a.w_search[2], gcd, maps, scp, ssep, L.cps_blocks); break;
+    default: k_loss_cps<4><<<grid, kCpsTX * kCpsTY, 0, st>>>(g, a.w_search[0], a.w_search[1], a.w_search[2], gcd, maps, scp, ssep, L.cps_blocks); break;
   }
-#undef QMIV_LOSS_CPS
   k_loss_sum_parts<<<a.n * 6, kSumThreads, 0, st>>>(ssep, L.cps_blocks, a.n * 6, sse, 1.0);
   k_loss_sum_parts<<<a.n * 6, kSumThreads, 0, st>>>(ssep + (size_t)a.n * 6 * L.cps_blocks, L.cps_blocks, a.n * 6,
                                            (double*)(a.ws + L.esum), 1.0);
