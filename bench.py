@@ -954,10 +954,13 @@ def run_ours(args):
             (Pws if erp else Pp).calc_frame(p0, p1, q.M_PSNR | q.M_WSPSNR | q.M_IVPSNR, sptr)
     plain_pass()
     torch.cuda.synchronize()
-    t = time.perf_counter()
-    plain_pass()
-    torch.cuda.synchronize()
-    plain_ms = (time.perf_counter() - t) * 1e3
+    plain_ms = []
+    for _ in range(2):
+        t = time.perf_counter()
+        plain_pass()
+        torch.cuda.synchronize()
+        plain_ms.append((time.perf_counter() - t) * 1e3)
+    plain_ms = min(plain_ms)
     plain_value = px_per_step / (plain_ms * 1e-3) / 1e9
 
     # ---- end to end: pinned host pictures through qmiv_calc_batch_host (uploads of each group
@@ -1029,7 +1032,8 @@ def run_ours(args):
                          "hbm_peak_kind": peak_kind, "traffic": traffic, "kernel": cps_name, "kernel_ms": cps_ms,
                          "peak_kind": "152 SMs x 128 INT32 lanes (x4 issue slots for issue_frac) x sampled SM clock"},
             "kernel_ms": kavg,
-            "plain": {"value": plain_value, "unit": "Gpixel/s", "batched_over_plain": value / world / plain_value},
+            "plain": {"value": plain_value, "unit": "Gpixel/s", "batched_over_plain": value / world / plain_value,
+                      "form": "one synchronous qmiv_calc_frame per pair, wall time of the 96 calls (best of 2)"},
             "graph": graph_line,
             "autotune": autotune,
             "check": {"ivpsnr_pair0": r0.ivpsnr, "gcd_pair0": list(r0.gcd_r2t)[:3]},

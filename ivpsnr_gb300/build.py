@@ -3,18 +3,22 @@
 * libqmiv_gb300.so : the CUDA kernels for sm_103a plus the C-ABI host code (nvcc).
 * libqmiv_synth.so : the deterministic synthetic-picture generator (host C).
 
-Translation units compile in parallel; objects go to ivpsnr_gb300/_build/ and are reused
-while newer than their sources and headers.
+Translation units compile in parallel; objects go to ivpsnr_gb300/_build/<machine>/ and are
+reused while newer than their sources and headers. A library or object built for another
+architecture (a working tree copied between an x86-64 and an aarch64 host) is never reused: the
+object folder is per machine, and a library whose ELF machine differs from the host's is rebuilt.
 """
 import concurrent.futures as cf
 import glob
 import os
+import platform
 import shutil
+import struct
 import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
-BUILD = os.path.join(HERE, "_build")
+BUILD = os.path.join(HERE, "_build", platform.machine() or "host")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 LIB = os.path.join(HERE, "libqmiv_gb300.so")
 SYNTH = os.path.join(HERE, "libqmiv_synth.so")
@@ -33,8 +37,25 @@ def _headers():
         glob.glob(os.path.join(INCLUDE, "*.h"))
 
 
+_ELF_MACHINE = {"x86_64": 62, "AMD64": 62, "aarch64": 183, "arm64": 183}
+
+
+def _foreign(path):
+    """True when path is an ELF file built for another machine than this host."""
+    want = _ELF_MACHINE.get(platform.machine())
+    try:
+        with open(path, "rb") as f:
+            head = f.read(20)
+    except OSError:
+        return False
+    if want is None or len(head) < 20 or head[:4] != b"\x7fELF":
+        return False
+    endian = "<" if head[5] == 1 else ">"
+    return struct.unpack(endian + "H", head[18:20])[0] != want
+
+
 def _stale(out, deps):
-    if not os.path.exists(out):
+    if not os.path.exists(out) or _foreign(out):
         return True
     t = os.path.getmtime(out)
     return any(os.path.getmtime(d) > t for d in deps)
@@ -75,7 +96,7 @@ def build(verbose=False, jobs=None):
             out = f.result()
             if verbose and out.strip():
                 print(out)
-    if steps or not os.path.exists(LIB):
+    if steps or not os.path.exists(LIB) or _foreign(LIB):
         _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart_static", "-lrt", "-ldl", "-lpthread"])
     return LIB
 
