@@ -96,8 +96,10 @@ def build(verbose=False, jobs=None):
             out = f.result()
             if verbose and out.strip():
                 print(out)
-    if steps or not os.path.exists(LIB) or _foreign(LIB):
-        _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart_static", "-lrt", "-ldl", "-lpthread"])
+    exports = os.path.join(CSRC, "exports.map")
+    if steps or not os.path.exists(LIB) or _foreign(LIB) or _stale(LIB, [exports]):
+        _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-Xlinker", "--version-script=" + exports,
+                                                              "-lcudart_static", "-lrt", "-ldl", "-lpthread"])
     return LIB
 
 

@@ -326,10 +326,10 @@ cudaError_t launch_generic(const DevJob* d, int n, int blocks, const Params& p, 
   return cudaGetLastError();
 }
 
-#define V420(SR, RPT, NWG, KT, K64, SUF) { "cps420_sr" #SR "_rpt" #RPT "_nwg" #NWG SUF, launch420<SR, RPT, NWG, KT>, \
+#define V420(SR, RPT, NWG, KT, K64, SUF) { "cps420_sr" #SR "_rpt" #RPT "_nwg" #NWG SUF, launch420<SR, RPT, NWG, KT>, launch420<SR, RPT, NWG, KT>, \
                                            SR, RPT * NWG, 64, K64, 1, 0 }
 const CpsVariant kVariants[] = {
-  { "cps_generic", launch_generic, 0, kGenTY, kGenTX, true, 0, 0 },
+  { "cps_generic", launch_generic, launch_generic, 0, kGenTY, kGenTX, true, 0, 0 },
   V420(1, 8, 2, unsigned int, false, "_k32"),
   V420(2, 8, 2, unsigned int, false, "_k32"),
   V420(2, 4, 2, unsigned int, false, "_k32"),

@@ -848,9 +848,14 @@ qmiv_status launch_jobs(qmiv_handle* h, const LaunchPlan& P, const uint8_t* d_ta
     {
       const CpsVariant& cv = variants()[P.sv[first]];
       int blocks = 0;
-      for(int i = first; i <= last; i++) blocks = h->jobs[i].cps_base + h->jobs[i].cps_strips * h->jobs[i].cps_segs;
+      bool maps = false;
+      for(int i = first; i <= last; i++)
+      {
+        blocks = h->jobs[i].cps_base + h->jobs[i].cps_strips * h->jobs[i].cps_segs;
+        maps = maps || h->jobs[i].cps_map[0] || h->jobs[i].cps_map[1];
+      }
       CUDA_TRY(prof_mark(h, cv.name, st, true));
-      if(blocks > 0) CUDA_TRY(cv.launch(d_jobs + first, last - first + 1, blocks, h->params, st));
+      if(blocks > 0) CUDA_TRY((maps ? cv.launch_map : cv.launch)(d_jobs + first, last - first + 1, blocks, h->params, st));
       CUDA_TRY(prof_mark(h, nullptr, st, false));
       h->launches++;
     }

@@ -98,6 +98,8 @@ cudaError_t launch_stats_static(const DevJob& j, const Params& p, cudaStream_t s
 struct CpsVariant {
   const char* name;
   cudaError_t (*launch)(const DevJob* d_jobs, int n, int blocks, const Params& p, cudaStream_t st);
+  // the same search for launches where some job writes argmin maps (DevJob::cps_map)
+  cudaError_t (*launch_map)(const DevJob* d_jobs, int n, int blocks, const Params& p, cudaStream_t st);
   int sr;        // search range it is specialised for (0: any)
   int rows;      // strip rows per block (generic: tile rows)
   int cols;      // columns per chunk (generic: tile columns)

@@ -34,6 +34,18 @@ def test_library_exports_every_declared_symbol(lib):
     assert not missing, missing
 
 
+def test_library_exports_nothing_but_the_c_abi(lib):
+    """The version script keeps launchers, kernel stubs and the static CUDA runtime local."""
+    import shutil
+    import subprocess
+    if not shutil.which("nm"):
+        pytest.skip("nm not available")
+    out = subprocess.run(["nm", "-D", "--defined-only", os.path.join(ROOT, "ivpsnr_gb300", "libqmiv_gb300.so")],
+                         stdout=subprocess.PIPE, text=True, check=True).stdout
+    funcs = {ln.split()[-1] for ln in out.splitlines() if len(ln.split()) == 3 and ln.split()[1] in "TW"}
+    assert funcs == _declared_symbols(), sorted(funcs ^ _declared_symbols())
+
+
 def test_python_binding_declares_every_symbol():
     from ivpsnr_gb300 import _abi
     declared = {n for n, _, _ in _abi.SIGNATURES}
