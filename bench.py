@@ -134,11 +134,14 @@ REF_TIMING = os.path.join(ROOT, "oracle", "_ref", "qmiv_ref_timing")
 
 
 def _write_pair(d, w, h, seed, frames=1, drift=False, shift_seed=0):
+    """Writes `frames` frames of a synthetic pair to two files; `seed` is the first frame's seed
+    (frame f takes seed + f) or a list of per-frame seeds."""
     from ivpsnr_gb300 import synth
     a, b = os.path.join(d, "a_%dx%d.yuv" % (w, h)), os.path.join(d, "b_%dx%d.yuv" % (w, h))
+    seeds = list(seed) if isinstance(seed, (list, tuple)) else [seed + f for f in range(frames)]
     with open(a, "wb") as fa, open(b, "wb") as fb:
         for f in range(frames):
-            ref, tst = synth.pair420(w, h, BD, seed=seed + f, holes=not drift, drift=drift, shift_seed=shift_seed, frame=f)
+            ref, tst = synth.pair420(w, h, BD, seed=seeds[f], holes=not drift, drift=drift, shift_seed=shift_seed, frame=f)
             fa.write(ref.astype("<u2").tobytes())
             fb.write(tst.astype("<u2").tobytes())
     return a, b
@@ -178,17 +181,21 @@ def ref_cli_ok():
     return _REF_CLI_OK
 
 
-def ref_cli_sample(pairs, metrics, sr=2, frames=1, drift=False):
+def ref_cli_sample(pairs, metrics, sr=2, frames=1, drift=False, weights=None):
     """Gpixel/s of the reference's processors over picture pairs [(w, h, erp, seed)], each written
-    to files and measured separately (one resolution per run, as the application takes it)."""
+    to files and measured separately (one resolution per run, as the application takes it); a
+    seed may be a list of per-frame seeds. weights[i] counts pair i that many times (a mix of
+    views represented by one pair per picture size)."""
     import tempfile
     px, secs, stages = 0, 0.0, []
     with tempfile.TemporaryDirectory() as d:
-        for (w, h, erp, seed) in pairs:
-            a, b = _write_pair(d, w, h, seed, frames, drift=drift, shift_seed=seed if drift else 0)
-            s, st = ref_cli_run(a, b, w, h, erp, sr, metrics, frames)
-            px += w * h
-            secs += s
+        for i, (w, h, erp, seed) in enumerate(pairs):
+            nf = len(seed) if isinstance(seed, (list, tuple)) else frames
+            a, b = _write_pair(d, w, h, seed, nf, drift=drift, shift_seed=seed if drift else 0)
+            s, st = ref_cli_run(a, b, w, h, erp, sr, metrics, nf)
+            k = nf * (weights[i] if weights else 1)
+            px += w * h * k
+            secs += s * k
             stages.append({"picture": "%dx%d%s" % (w, h, " ERP" if erp else ""), "ms": st})
             os.unlink(a)
             os.unlink(b)
@@ -212,7 +219,8 @@ def headline_in_bytes(jobs):
 def run_reference(args):
     """The reference's own CPU implementation of the path on all host threads: its metric library
     built for this machine and driven as the application drives it (the oracle port where that
-    build is absent), one picture pair of the multiview workload per step, views cycled."""
+    build is absent), views of the multiview workload cycled: one view's 8 frames per step through
+    the reference's library, one picture pair per step through the port."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
@@ -224,9 +232,9 @@ def run_reference(args):
 
     def step(i):
         v, f, w, h, erp = jobs[(i * FRAMES) % len(jobs)]
-        if use_cli:
-            _, secs, _ = ref_cli_sample([(w, h, erp, synth.seed_for(1, v, f))], metrics)
-            return w * h, secs
+        if use_cli:  # one view's 8 frames
+            _, secs, _ = ref_cli_sample([(w, h, erp, [synth.seed_for(1, v, k) for k in range(FRAMES)])], metrics)
+            return w * h * FRAMES, secs
         from oracle import oracle as oq
         ref, tst = synth.pair420(w, h, BD, seed=synth.seed_for(1, v, f), holes=True)
         p0 = oq.upsample420(synth.split420(ref, w, h), w, h)
@@ -245,7 +253,7 @@ def run_reference(args):
     val = px / secs / 1e9
     if use_cli:
         kind = "reference"
-        sample = ("one picture pair per step (views cycled), the reference's metric library built from its sources "
+        sample = ("one view (8 frames) per step, views cycled, the reference's metric library built from its sources "
                   "for this host (%s), all host threads, per-frame time of PREPROC+GCD+PSNR+WS-PSNR+IV-PSNR "
                   "(oracle/ref_timing.cpp)" % os.uname().machine)
     else:
@@ -262,9 +270,9 @@ def run_reference(args):
 
 
 def cpu_baseline_sample():
-    """Bounded CPU sample for the GPU line: two pairs of the workload (one ERP 4096x2048, one
-    1920x1080) through the reference's own metric library on all host threads, and the oracle port
-    beside it."""
+    """CPU baseline for the GPU line: the whole step (the 12 views x 8 frames, 96 pairs) through the
+    reference's own metric library on all host threads, and the oracle port beside it on a bounded
+    sample (two pairs)."""
     from ivpsnr_gb300 import synth
     from oracle import oracle as oq
     nth = host_threads()
@@ -282,12 +290,13 @@ def cpu_baseline_sample():
             "sample": "2 of 96 picture pairs (4096x2048 ERP + 1920x1080), GCD+PSNR+WS-PSNR+IV-PSNR, oracle/ C port"}
     if not ref_cli_ok():
         return port
-    val, rsecs, stages = ref_cli_sample(pairs, ["psnr", "wspsnr", "ivpsnr"])
+    views = [(w, h, erp, [synth.seed_for(1, v, f) for f in range(FRAMES)]) for v, (w, h, erp) in enumerate(VIEWS)]
+    val, rsecs, stages = ref_cli_sample(views, ["psnr", "wspsnr", "ivpsnr"])
     return {"value": val, "unit": "Gpixel/s", "cores": nth, "kind": "reference",
-            "sample": "2 of 96 picture pairs (4096x2048 ERP + 1920x1080) through the reference's metric library "
-                      "built for this host (%s), all host threads, per-frame time of PREPROC+GCD+PSNR+WS-PSNR+IV-PSNR "
-                      "(oracle/ref_timing.cpp)" % os.uname().machine,
-            "seconds": rsecs, "stages_ms": stages, "port": port}
+            "sample": "the whole step: all 96 picture pairs (12 views x 8 frames, one run per view) through the "
+                      "reference's metric library built for this host (%s), all host threads, per-frame time of "
+                      "PREPROC+GCD+PSNR+WS-PSNR+IV-PSNR (oracle/ref_timing.cpp)" % os.uname().machine,
+            "seconds": rsecs, "stages_ms": stages[:1] + stages[3:4] + stages[9:10], "port": port}
 
 
 SSIM_WORKLOAD = "ivssim-ssim-msssim-10bit-420: 17 frames 1920x1080, drifting block shifts, SR 2, REF10 window"
@@ -378,13 +387,13 @@ def ssim_workload(args, dev, stream):
            "quad_outputs": nf * 3 * max(0, w - 10) * max(0, h - 10),
            "check": {"ivssim_frame0": r0.ivssim, "ssim_frame0": list(r0.ssim)[:3]}}
     if not args.no_cpu_baseline and ref_cli_ok():
-        val, secs, st = ref_cli_sample([(w, h, False, synth.seed_for(2, 0, 0))], ["ssim", "msssim", "ivssim"], frames=2,
+        val, secs, st = ref_cli_sample([(w, h, False, synth.seed_for(2, 0, 0))], ["ssim", "msssim", "ivssim"], frames=nf,
                                        drift=True)
         out["cpu_baseline"] = {"value": val, "unit": "Gpixel/s", "cores": host_threads(), "kind": "reference",
-                               "sample": "frames 0-1 of the 17 through the reference's metric library (%s), all host "
-                                         "threads, per-frame time of PREPROC+GCD+SCP+SSIM+MS-SSIM+IV-SSIM"
-                                         % os.uname().machine,
-                               "seconds_per_frame": secs, "stages_ms": st}
+                               "sample": "the whole step: all %d frames through the reference's metric library (%s), "
+                                         "all host threads, per-frame time of PREPROC+GCD+SCP+SSIM+MS-SSIM+IV-SSIM"
+                                         % (nf, os.uname().machine),
+                               "seconds": secs, "stages_ms": st}
     return out
 
 
@@ -489,12 +498,15 @@ def multiview_ivssim_workload(args, dev, stream, jobs, host, devbufs, planes):
            "kernel_ms": kt, "quad_outputs": quad_outputs,
            "check": {"ivpsnr_pair0": r0.ivpsnr, "ivssim_pair0": r0.ivssim, "msssim_pair0": list(r0.msssim)[:3]}}
     if not args.no_cpu_baseline and ref_cli_ok():
-        pairs = [(4096, 2048, True, synth.seed_for(1, 0, 0)), (1920, 1080, False, synth.seed_for(1, 3, 0))]
-        val, rsecs, st = ref_cli_sample(pairs, ["psnr", "wspsnr", "ivpsnr", "ssim", "msssim", "ivssim"])
+        pairs = [(4096, 2048, True, synth.seed_for(1, 0, 0)), (1920, 1080, False, synth.seed_for(1, 3, 0)),
+                 (2048, 1088, False, synth.seed_for(1, 9, 0))]
+        counts = [sum(1 for v in VIEWS if v[:2] == p[:2]) for p in pairs]
+        val, rsecs, st = ref_cli_sample(pairs, ["psnr", "wspsnr", "ivpsnr", "ssim", "msssim", "ivssim"], weights=counts)
         out["cpu_baseline"] = {"value": val, "unit": "Gpixel/s", "cores": host_threads(), "kind": "reference",
-                               "sample": "2 of 96 picture pairs (4096x2048 ERP + 1920x1080) through the reference's "
-                                         "metric library (%s), all host threads, all six metrics, per-frame time "
-                                         "of the path steps" % os.uname().machine,
+                               "sample": "one pair of each picture size (4096x2048 ERP, 1920x1080, 2048x1088) through "
+                                         "the reference's metric library (%s), all host threads, all six metrics, "
+                                         "weighted 3:6:3 as the views of the step, per-frame time of the path "
+                                         "steps" % os.uname().machine,
                                "seconds": rsecs, "stages_ms": st}
     return out
 
