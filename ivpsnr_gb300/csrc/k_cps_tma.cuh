@@ -56,8 +56,9 @@ struct TGeo {
   static constexpr int CVT  = 2 * TH * TW * 4 * CE;
   static constexpr int ACC  = 2 * R * 3 * 8;
   static constexpr int SMEM = 2 * STAGE + CVT + ACC + 32;    // + 3 mbarriers
-  // resident blocks the register budget is sized for: 24 warps per SM at search range <= 2
-  static constexpr int MINB = SR <= 2 ? 768 / NT : 512 / NT;
+  // resident blocks the register budget is sized for: 20 warps per SM at search range <= 2 (the
+  // shared memory of the 128-thread shapes holds five blocks, so a tighter budget buys nothing)
+  static constexpr int MINB = SR <= 2 ? 640 / NT : 512 / NT;
   static_assert(SR <= XA, "halo wider than the box alignment pad");
   static_assert(RW <= 256 && TH <= 256 && CRW <= 256 && CTH <= 256, "tensor box too large");
 };
@@ -368,13 +369,19 @@ k_cps420_tma(const DevJob* __restrict__ jobs, int njobs, Params p)
             const unsigned k = p.key_m_log2 >= 0 ? (unsigned)(best[a][px] & (KeyT)(p.key_m - 1))
                                                  : (unsigned)(best[a][px] % (KeyT)p.key_m);
             const int dy = (int)(k >> G::KS_LOG2) - SR, dx = (int)(k & (G::KS - 1)) - SR;
-            const int rl = cvtR[((2 * qr + a + SR + dy) * G::TW + 2 * lane + px + SR + dx) * CE];
+            // the argmin's reference luma: from the raw 16-bit box inside the picture (one
+            // shared-memory wavefront per warp), from the clamped, scaled tile at the edges
+            int rl;
+            if constexpr(IN)
+              rl = reinterpret_cast<const T*>(sb + rp * G::LBOX)[(2 * qr + a + SR + dy) * G::RW + 2 * lane + px + dx + G::XA];
+            else
+              rl = cvtR[((2 * qr + a + SR + dy) * G::TW + 2 * lane + px + SR + dx) * CE];
             const int crow = (IN ? qc + ((a + dy) >> 1) : clampi(qc + ((a + dy) >> 1), 0, Hc - 1)) - cry0;
             const int ccl = (IN ? cxh + lane + ((px + dx) >> 1) : clampi(cxh + lane + ((px + dx) >> 1), 0, Wc - 1)) - crx0;
             const int rcb = chrR0[crow * G::CRW + ccl], rcr = chrR1[crow * G::CRW + ccl];
             int rY, tYr;
-            if(p.luma_scale_log2 >= 0) { rY = rl >> p.luma_scale_log2; tYr = tY[a][px] >> p.luma_scale_log2; }
-            else                       { rY = rl / s; tYr = tY[a][px] / s; }
+            if(p.luma_scale_log2 >= 0) { rY = IN ? rl : rl >> p.luma_scale_log2; tYr = tY[a][px] >> p.luma_scale_log2; }
+            else                       { rY = IN ? rl : rl / s; tYr = tY[a][px] / s; }
             const int d0 = tYr - rY, d1 = tCb - rcb, d2 = tCr - rcr;
             if(IN)
             {
