@@ -400,6 +400,8 @@ void plan_grid(qmiv_handle* h, DevJob* jobs, int n, const std::vector<int>& vari
     const int max_chunks = std::max(1, (int)std::floor(4294967295.0 / (2.0 * D * D)));
     int seg_chunks = (nchunks + segs - 1) / segs;
     if(seg_chunks > max_chunks) seg_chunks = max_chunks;
+    // at most 16 chunks (1024 columns) per block: the last wave of a launch stays short
+    if(seg_chunks > 16) seg_chunks = 16;
     j.cps_seg_chunks = seg_chunks;
     j.cps_segs = (nchunks + seg_chunks - 1) / seg_chunks;
   }
