@@ -13,7 +13,8 @@
 //     reference rows x 2 output rows x 2 columns x (2B+1) candidates of one
 //     multiply-add + add + unsigned min each;
 //   * per-row squared errors are reduced with a single warp reduction per row and
-//     component and accumulated in shared memory, then added to the job's row sums.
+//     component per chunk, kept in one lane's register for the whole block, and added to the
+//     job's row sums once at the end.
 //
 // The kernel is instantiated twice per variant: without argmin-map writes (k_cps_tma.cu, every
 // metric call) and with them (k_cps_tma_map.cu, qmiv_cps_maps), in separate translation units
@@ -130,6 +131,13 @@ k_cps420_tma(const DevJob* __restrict__ jobs, int njobs, Params p)
 
   bool failed = false;
   int it = 0;
+  // Per-row squared errors: a warp owns the same 2 QPW rows of its direction in every chunk, so
+  // each (quad, row, component) sum of the block lives in one lane's register (lane
+  // 6 qi + 3 a + c), which takes the warp's reduction of that sum per chunk; the lanes write
+  // them to shared memory once, after the last chunk. Shapes with more than 32 such sums per
+  // warp add each reduction to shared memory instead.
+  constexpr bool kLaneSums = 6 * QPW <= 32;
+  unsigned long long lacc = 0;
   for(int ch = ch0; ch < ch1; ch++, it++)
   {
     const int stg = it & 1;
@@ -414,17 +422,23 @@ k_cps420_tma(const DevJob* __restrict__ jobs, int njobs, Params p)
               scp[2][o] = (uint16_t)clampi(sv[a][px][2] - gd2, 0, mx);
             }
         }
-        #pragma unroll
-        for(int a = 0; a < 2; a++)
+        {
+          const int t = lane - 6 * qi;  // which of the quad's six sums this lane keeps, if any
+          unsigned long long pick = 0;
           #pragma unroll
-          for(int c = 0; c < 3; c++)
-          {
-            unsigned long long v;
-            if(sizeof(KeyT) == 4) v = __reduce_add_sync(0xffffffffu, sq[a][c]);
-            else v = ((unsigned long long)__reduce_add_sync(0xffffffffu, sq[a][c] >> 16) << 16) +
-                     __reduce_add_sync(0xffffffffu, sq[a][c] & 0xFFFFu);
-            if(lane == 0) acc[(dir * G::R + 2 * qr + a) * 3 + c] += v;
-          }
+          for(int a = 0; a < 2; a++)
+            #pragma unroll
+            for(int c = 0; c < 3; c++)
+            {
+              unsigned long long v;
+              if(sizeof(KeyT) == 4) v = __reduce_add_sync(0xffffffffu, sq[a][c]);
+              else v = ((unsigned long long)__reduce_add_sync(0xffffffffu, sq[a][c] >> 16) << 16) +
+                       __reduce_add_sync(0xffffffffu, sq[a][c] & 0xFFFFu);
+              if constexpr(kLaneSums) pick = t == a * 3 + c ? v : pick;
+              else if(lane == 0) acc[(dir * G::R + 2 * qr + a) * 3 + c] += v;
+            }
+          if constexpr(kLaneSums) lacc += pick;
+        }
       }
       };
       if(interior) run_quads(std::true_type{});
@@ -433,6 +447,11 @@ k_cps420_tma(const DevJob* __restrict__ jobs, int njobs, Params p)
     __syncthreads();
   }
 
+  if(kLaneSums && lane < 6 * QPW)
+  {
+    const int qi = lane / 6, rem = lane - 6 * qi, a = rem / 3, c = rem - 3 * a;
+    acc[(dir * G::R + 2 * (wg * QPW + qi) + a) * 3 + c] = lacc;
+  }
   if(failed && tid == 0)
   { // let the copies in flight land before the block's shared memory is released
     const int stg = it & 1;
