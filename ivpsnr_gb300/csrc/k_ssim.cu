@@ -802,7 +802,7 @@ template <int WIN> struct BGeo {
                                                      // they are consumed, the new transposed sums (pitch FP)
   static constexpr int S_M = kBwdT * MP * 16;        // coefficient maps of the new position rows
   static constexpr int SMEM = S_SMP + S_K + S_V + S_M;
-  static_assert(4 * SW <= 256 && 32 * ((PW + 7) / 8) <= 256 && KR <= kBwdT && FP <= VP, "one round of the block per pass");
+  static_assert(4 * SW <= 256 && 32 * ((PW + 5) / 6) <= 256 && KR <= kBwdT && FP <= VP, "one round of the block per pass");
 };
 
 // acc += g * v on a float4 as two packed FP32 multiply-adds
@@ -813,14 +813,14 @@ __device__ __forceinline__ void fma4(float2 g, const float4& v, float4& acc)
   acc = make_float4(lo.x, lo.y, hi.x, hi.y);
 }
 
-// Each pass is register-blocked: a thread filters 8 (the last one 4) consecutive outputs along
-// the pass direction from that many + WIN - 1 shared-memory reads.
+// Each pass is register-blocked: a thread filters 4 to 8 consecutive outputs along the pass
+// direction from that many + WIN - 1 shared-memory reads.
 template <int WIN>
 __global__ void __launch_bounds__(256, 3) k_ssim_bwd(const SsimBwdJob* __restrict__ jobs, int njobs)
 {
   using G = BGeo<WIN>;
   constexpr int PW = G::PW, SW = G::SW, KR = G::KR, SR = G::SR, VP = G::VP, MP = G::MP, FP = G::FP, K1 = G::K1;
-  constexpr int NG = (PW + 7) / 8;
+  constexpr int MG = 6, NG = (PW + MG - 1) / MG;  // map pass: MG position columns per thread
   extern __shared__ __align__(16) float smem[];
   float2* s_s = reinterpret_cast<float2*>(smem);                                      // [SR][SW]
   // transposed horizontal sums [SR][FP]: the KR kept rows directly before the vertical-moment
@@ -915,28 +915,29 @@ __global__ void __launch_bounds__(256, 3) k_ssim_bwd(const SsimBwdJob* __restric
     }
     __syncthreads();
     // horizontal moments -> coefficient maps (zero outside the valid region): thread = position
-    // row x 8 consecutive position columns
+    // row x 6 consecutive position columns (32 x 7 items: 7 of the block's 8 warps; groups of 8
+    // columns left two warps idle at the next barrier)
     {
       const float k_cc = s_kcc;
       for(int it = tid; it < kBwdT * NG; it += 256)
       {
-        const int r = it % kBwdT, c0 = min(8 * (it / kBwdT), PW - 8);
+        const int r = it % kBwdT, c0 = min(MG * (it / kBwdT), PW - MG);
         if(prime && r < kBwdT - KR) continue;
-        float4 acc[8];
+        float4 acc[MG];
         #pragma unroll
-        for(int o = 0; o < 8; o++) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for(int o = 0; o < MG; o++) acc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
         #pragma unroll
-        for(int i = 0; i < 7 + WIN; i++)
+        for(int i = 0; i < MG - 1 + WIN; i++)
         {
           const float4 v = s_v[r * VP + c0 + i];
           #pragma unroll
-          for(int o = 0; o < 8; o++)
+          for(int o = 0; o < MG; o++)
             if(i - o >= 0 && i - o < WIN) fma4(gk[i - o], v, acc[o]);
         }
         const int py = y + 5 + r;
         const bool row_ok = py >= 5 && py < H - 5;
         #pragma unroll
-        for(int o = 0; o < 8; o++)
+        for(int o = 0; o < MG; o++)
         {
           const int px = px0 + c0 + o;
           float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
