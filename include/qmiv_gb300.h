@@ -216,9 +216,9 @@ qmiv_status qmiv_psnr(qmiv_handle* h, const qmiv_pic* pic0, const qmiv_pic* pic1
  * QMIV_BAD_ARG. opt may be null
  * (defaults); it supplies unnoticeable, cmp_w_avg and fake_exact. Fills out->psnr,
  * psnr_pic, gcd_r2t and exact; every other field is 0. Synchronous on `stream`.
- * The first call on each device looks up the static array's address and should be made
- * before any stream capture begins. All callers on a device share the one array: calls that
- * overlap in time, from other threads or on other streams, race and must be serialised. */
+ * The first call on each device looks up the static array's address. All callers on a
+ * device share the one array: calls that overlap in time, from other threads or on other
+ * streams, race and must be serialised. */
 qmiv_status qmiv_psnr_static(const qmiv_pic* pic0, const qmiv_pic* pic1, const qmiv_options* opt,
                              qmiv_frame_result* out, qmiv_stream stream);
 /* xIVPSNR::calcPicIVPSNR(Tst=P0, Ref=P1, GCD) (xIVPSNR.cpp:32-56); gcd_r2t may be null (computed) */
