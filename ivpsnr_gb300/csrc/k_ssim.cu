@@ -39,16 +39,16 @@ namespace {
 // Tile geometry. A persistent block of 256 threads walks the tiles of all jobs; per tile it
 // stages a 64-column strip of IH rows of both planes as (a, b) pairs, filters it vertically
 // into TY output rows (thread = staged column x 8 output rows), then horizontally (thread =
-// output row x 8 output columns) and evaluates the index.
-constexpr int kThreads = 256, kIW = 64, kTY = 32, kRP = 67;
+// output row x 7 output columns, all eight warps) and evaluates the index.
+constexpr int kThreads = 256, kIW = 64, kTY = 32, kRP = 66, kHO = 7;
 template <int WIN> struct SGeo {
   static constexpr int TX = kIW - WIN + 1;          // 55 output columns (REF10), 54 (GAUSS11)
   static constexpr int IH = kTY + WIN - 1;          // staged rows
   static constexpr int RPW = (IH + 7) / 8;          // staged rows per warp
   // staged (a, b) pairs [IH][64] float2; vertical moments [32][kRP] float4 (S1a, S1b,
-  // S(a^2+b^2), S(ab)) with an odd pitch (conflict-free reads down a column); row sums [7][32]
-  static constexpr int SMEM = IH * kIW * 8 + kTY * kRP * 16 + 7 * kTY * 4;
-  static_assert(8 * 7 >= TX && 8 * 6 + 7 + WIN - 1 < kRP, "tile columns");
+  // S(a^2+b^2), S(ab))
+  static constexpr int SMEM = IH * kIW * 8 + kTY * kRP * 16;
+  static_assert(8 * kHO >= TX && 8 * kHO + WIN - 2 < kRP, "tile columns");
 };
 
 __device__ __forceinline__ float ld_plane(const SsimPlane& p, int x, int y)
@@ -114,7 +114,6 @@ __global__ void __launch_bounds__(kThreads, 3) k_ssim(const SsimJob* __restrict_
   __shared__ float s_kcc;  // (1 - W0) tc^2 W0 of the current tile, formed in FP64 by one thread
   float2* s_in = reinterpret_cast<float2*>(smem);                    // [IH][64]
   float4* s_v = reinterpret_cast<float4*>(smem + 2 * G::IH * kIW);   // [32][kRP]
-  float* s_red = smem + 2 * G::IH * kIW + 4 * kTY * kRP;             // [7][32]
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   // window factor pairs (g, g), kept in registers for the whole kernel
@@ -182,20 +181,21 @@ __global__ void __launch_bounds__(kThreads, 3) k_ssim(const SsimJob* __restrict_
     }
     __syncthreads();
 
-    // horizontal pass and the index: warp w takes output columns 8w .. 8w+7, lane = output row
-    if(warp < 7)
+    // horizontal pass and the index: thread = output row r x outputs 7g .. 7g+6 (g = 0..7); lanes
+    // 4g + i of warp w hold row 4w + i, so a row's eight groups reduce by shuffles. The float4
+    // pitch kRP = 2 mod 8 keeps the reads of a quarter-warp on distinct bank groups.
     {
-      const int o = lane, j0 = 8 * warp;
+      const int g = lane >> 2, o = 4 * warp + (lane & 3), j0 = kHO * g;
       const float4* src = s_v + o * kRP + j0;
-      float2 m1[8], m2[8];
+      float2 m1[kHO], m2[kHO];
       #pragma unroll
-      for(int jj = 0; jj < 8; jj++) { m1[jj] = make_float2(0.f, 0.f); m2[jj] = make_float2(0.f, 0.f); }
+      for(int jj = 0; jj < kHO; jj++) { m1[jj] = make_float2(0.f, 0.f); m2[jj] = make_float2(0.f, 0.f); }
       #pragma unroll
-      for(int t = 0; t < 7 + WIN; t++)
+      for(int t = 0; t < kHO - 1 + WIN; t++)
       {
         const float4 val = src[t];
         #pragma unroll
-        for(int jj = 0; jj < 8; jj++)
+        for(int jj = 0; jj < kHO; jj++)
         {
           const int k = t - jj;
           if(k < 0 || k >= WIN) continue;
@@ -211,7 +211,7 @@ __global__ void __launch_bounds__(kThreads, 3) k_ssim(const SsimJob* __restrict_
       const bool row_ok = y0 + o < y1;
       float rs = 0.0f;
       #pragma unroll
-      for(int jj = 0; jj < 8; jj++)
+      for(int jj = 0; jj < kHO; jj++)
       {
         const float S1a = m1[jj].x, S1b = m1[jj].y, Sq = m2[jj].x, Sx = m2[jj].y;
         const float sab = S1a + S1b;
@@ -227,19 +227,15 @@ __global__ void __launch_bounds__(kThreads, 3) k_ssim(const SsimJob* __restrict_
         }
         rs += (row_ok && x0 + j0 + jj < x1) ? __fdividef(num, den) : 0.0f;
       }
-      s_red[warp * kTY + o] = rs;
+      // fixed-order sum over the row's eight groups
+      rs += __shfl_xor_sync(0xffffffffu, rs, 4);
+      rs += __shfl_xor_sync(0xffffffffu, rs, 8);
+      rs += __shfl_xor_sync(0xffffffffu, rs, 16);
+      if(g == 0 && row_ok) J.partial[(int64_t)(y0 + o - 5) * J.tiles_x + tx] = rs;
     }
     __syncthreads();
-    if(tid < kTY)
-    { // row tid of the tile: fixed-order sum over the 7 column groups
-      float s = 0.0f;
-      #pragma unroll
-      for(int w = 0; w < 7; w++) s += s_red[w * kTY + tid];
-      const int y = y0 + tid;
-      if(y < y1) J.partial[(int64_t)(y - 5) * J.tiles_x + tx] = s;
-    }
-    // the next tile's staging overwrites s_in only; s_v and s_red are rewritten after two
-    // more barriers
+    // the next tile's staging overwrites s_in and s_kcc after the barrier above; s_v is
+    // rewritten after one more
   }
 }
 
