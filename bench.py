@@ -457,15 +457,18 @@ def multiview_ivssim_workload(args, dev, stream, jobs, host, devbufs, planes):
     def e2e_step():
         P.calc_batch_host(hjobs, res.data_ptr(), 0, sptr)
         res_host.copy_(res, non_blocking=True)
-    for _ in range(max(1, args.warmup // 2)):
+    for _ in range(max(2, args.warmup)):
         e2e_step()
     torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(args.steps):
-        e2e_step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
+    e2e_passes = []  # two passes, the faster reported (as for the headline's end-to-end figure)
+    for _ in range(2):
+        e0.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_passes.append(e0.elapsed_time(e1) / args.steps)
+    e2e_ms = min(e2e_passes)
     P.close()
     # plain form: one synchronous call per pair
     Pp = q.Processor(4096, 2048, max_jobs=1, scratch_metrics=metrics)
@@ -492,7 +495,7 @@ def multiview_ivssim_workload(args, dev, stream, jobs, host, devbufs, planes):
            "gpu_launches": launches,
            "plain_value": px / (plain_ms * 1e-3) / 1e9, "batched_over_plain": plain_ms / ms,
            "plain": "one synchronous qmiv_calc_frame per pair, wall time of the 96 calls (best of 2)",
-           "e2e": {"value": px / (e2e_ms * 1e-3) / 1e9, "unit": "Gpixel/s", "ms_per_step": e2e_ms,
+           "e2e": {"value": px / (e2e_ms * 1e-3) / 1e9, "unit": "Gpixel/s", "ms_per_step": e2e_ms, "passes_ms": e2e_passes,
                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": n * rsz,
                    "call": "qmiv_calc_batch_host (pinned host pictures, grouped uploads overlapped with compute)"},
            "kernel_ms": kt, "quad_outputs": quad_outputs,
@@ -990,16 +993,22 @@ def run_ours(args):
     def e2e_step():
         P.calc_batch_host(hjobs, res_dev.data_ptr(), 0, sptr)
         res_host.copy_(res_dev, non_blocking=True)
-    for _ in range(max(1, args.warmup // 2)):
+    for _ in range(max(2, args.warmup)):
         e2e_step()
     torch.cuda.synchronize()
-    barrier()
-    e0.record(stream)
-    for _ in range(args.steps):
-        e2e_step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
+    # two timed passes of K steps, the faster one reported (both listed): the host link and host
+    # memory of this shared machine see other tenants' traffic, which moved single passes by up
+    # to a factor of two between otherwise identical processes
+    e2e_passes = []
+    for _ in range(2):
+        barrier()
+        e0.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_passes.append(e0.elapsed_time(e1) / args.steps)
+    e2e_ms = min(e2e_passes)
     barrier()
     if world > 1:
         t = torch.tensor([e2e_ms], device=dev)
@@ -1028,7 +1037,7 @@ def run_ours(args):
             "config": headline_config(jobs, in_bytes),
             "clocks": clk,
             "e2e": {"value": e2e_value, "unit": "Gpixel/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": nres * rsz, "ms_per_step": e2e_ms,
+                    "d2h_bytes_per_step": nres * rsz, "ms_per_step": e2e_ms, "passes_ms": e2e_passes,
                     "call": "qmiv_calc_batch_host (pinned host pictures, grouped uploads overlapped with compute)"},
             "gpu_launches": gpu_launches,
             # the search kernel is bound by integer instruction issue: three views side by side.
