@@ -652,11 +652,15 @@ __global__ void __launch_bounds__(kQThreads, 1) k_ssim_quad(const SsimQuadJob* _
   }
 }
 
-// Picture sum of one SSIM job (xSSIM.cpp:106-111): a thread per row adds the row's per-tile sums
-// in order as an exact FP32 pair (TwoSum), the row value goes to FP64 once, rows are combined
-// with a compensated sum in a fixed order, and the picture sum is divided by W*H. FP32 pairs
-// rather than FP64 adds per tile: GB300's FP64 rate made the per-tile adds the cost of this
-// kernel on large pictures.
+// Picture sum of one SSIM job (xSSIM.cpp:106-111), in two passes. Row pass: a warp per row adds
+// the row's per-tile sums as an FP32 pair (TwoSum), lane t taking tiles t, t + 32, ... in order,
+// and the lanes' pairs are combined by a fixed butterfly of TwoSums (every lane ends with the
+// same pair: TwoSum's error term is exact whatever the order of its operands); the pair replaces
+// the row's first two tile sums (a one-tile row keeps its value). Job pass: the row values go to
+// FP64 once, are combined with a compensated sum in a fixed order, and the picture sum is
+// divided by W*H. FP32 pairs rather than FP64 adds per tile: GB300's FP64 rate made the per-tile
+// adds the cost of this step on large pictures. The row pass spreads a job over several blocks:
+// a block per job with a thread per row took 0.27 ms for an 8K frame's 21 jobs on 21 SMs.
 __device__ __forceinline__ void fin_two_sum(float a, float b, float& s, float& e)
 {
   s = __fadd_rn(a, b);
@@ -664,34 +668,44 @@ __device__ __forceinline__ void fin_two_sum(float a, float b, float& s, float& e
   e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 
-constexpr int kFinThreads = 512;
-__global__ void __launch_bounds__(kFinThreads) k_ssim_finalize(const SsimJob* __restrict__ jobs, int njobs)
+constexpr int kFinThreads = 256, kFinWarps = kFinThreads / 32;
+__global__ void __launch_bounds__(kFinThreads) k_ssim_fin_rows(const SsimJob* __restrict__ jobs)
 {
-  __shared__ double scratch[2 * (kFinThreads / 32)];
+  const SsimJob& J = jobs[blockIdx.y];
+  const int rows = max(0, J.H - 10), tx = J.tiles_x;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for(int r = blockIdx.x * kFinWarps + w; r < rows; r += gridDim.x * kFinWarps)
+  {
+    float* pr = J.partial + (int64_t)r * tx;
+    float hi = 0.0f, lo = 0.0f;
+    for(int t = lane; t < tx; t += 32)
+    {
+      float e;
+      fin_two_sum(hi, __ldcg(pr + t), hi, e);
+      lo = __fadd_rn(lo, e);
+    }
+    #pragma unroll
+    for(int off = 16; off; off >>= 1)
+    {
+      const float h2 = __shfl_xor_sync(0xffffffffu, hi, off), l2 = __shfl_xor_sync(0xffffffffu, lo, off);
+      float e;
+      fin_two_sum(hi, h2, hi, e);
+      lo = __fadd_rn(__fadd_rn(lo, l2), e);
+    }
+    if(lane == 0 && tx >= 2) { pr[0] = hi; pr[1] = lo; }
+  }
+}
+
+__global__ void __launch_bounds__(kFinThreads) k_ssim_fin_jobs(const SsimJob* __restrict__ jobs)
+{
+  __shared__ double scratch[2 * kFinWarps];
   const SsimJob& J = jobs[blockIdx.x];
-  const int rows = max(0, J.H - 10);
+  const int rows = max(0, J.H - 10), tx = J.tiles_x;
   Kbns k = { 0.0, 0.0 };
   for(int r = threadIdx.x; r < rows; r += kFinThreads)
   {
-    const float* pr = J.partial + (int64_t)r * J.tiles_x;
-    float hi = 0.0f, lo = 0.0f;
-    // eight loads in flight ahead of the (serial) pair additions, in the same order
-    constexpr int kB = 8;
-    for(int t0 = 0; t0 < J.tiles_x; t0 += kB)
-    {
-      float v[kB];
-      #pragma unroll
-      for(int j = 0; j < kB; j++) v[j] = t0 + j < J.tiles_x ? __ldcg(pr + t0 + j) : 0.0f;
-      #pragma unroll
-      for(int j = 0; j < kB; j++)
-      {
-        if(t0 + j >= J.tiles_x) break;
-        float e;
-        fin_two_sum(hi, v[j], hi, e);
-        lo = __fadd_rn(lo, e);
-      }
-    }
-    k = kbns_add(k, __dadd_rn((double)hi, (double)lo));
+    const float* pr = J.partial + (int64_t)r * tx;
+    k = kbns_add(k, tx >= 2 ? __dadd_rn((double)__ldcg(pr), (double)__ldcg(pr + 1)) : (double)__ldcg(pr));
   }
   const double tot = block_kbns(k, scratch);
   if(threadIdx.x == 0) *J.out = __ddiv_rn(tot, (double)((int64_t)J.W * J.H));
@@ -1046,6 +1060,18 @@ int ssim_tiles_x(int W, int window)
 }
 int ssim_tiles_y(int H) { return H > 10 ? (H - 10 + kTY - 1) / kTY : 0; }
 
+cudaError_t launch_ssim_finalize(const SsimJob* d_jobs, const SsimJob* h_jobs, int n, cudaStream_t st)
+{
+  if(n <= 0) return cudaSuccess;
+  int rows = 0;
+  for(int i = 0; i < n; i++) rows = std::max(rows, h_jobs[i].H - 10);
+  // row-pass blocks per job: about 16 rows per warp for the tallest job, at most 8
+  const int per_job = std::min(8, std::max(1, (rows + 16 * kFinWarps - 1) / (16 * kFinWarps)));
+  k_ssim_fin_rows<<<dim3(per_job, n), kFinThreads, 0, st>>>(d_jobs);
+  k_ssim_fin_jobs<<<n, kFinThreads, 0, st>>>(d_jobs);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_ssim(const SsimJob* d_jobs, const SsimJob* h_jobs, int n, int window, cudaStream_t st)
 {
   int tiles = 0;
@@ -1074,8 +1100,7 @@ cudaError_t launch_ssim(const SsimJob* d_jobs, const SsimJob* h_jobs, int n, int
     cudaError_t e = cudaGetLastError();
     if(e != cudaSuccess) return e;
   }
-  k_ssim_finalize<<<n, kFinThreads, 0, st>>>(d_jobs, n);
-  return cudaGetLastError();
+  return launch_ssim_finalize(d_jobs, h_jobs, n, st);
 }
 
 int ssim_bwd_tiles(int dim) { return (dim + kBwdT - 1) / kBwdT; }

@@ -826,6 +826,14 @@ qmiv_status plan_jobs(qmiv_handle* h, LaunchPlan& P, cudaStream_t st)
   return QMIV_OK;
 }
 
+// Tiles of the SSIM tile kernel in a job table (0: it is not launched).
+int ssim_tiles(const std::vector<SsimJob>& sj)
+{
+  int t = 0;
+  for(const SsimJob& j : sj) t = std::max(t, j.tile_base + j.tiles_x * j.tiles_y);
+  return t;
+}
+
 // Every launch of a plan, reading its tables from d_tab (laid out by pack_tables).
 qmiv_status launch_jobs(qmiv_handle* h, const LaunchPlan& P, const uint8_t* d_tab, cudaStream_t st)
 {
@@ -893,7 +901,7 @@ qmiv_status launch_jobs(qmiv_handle* h, const LaunchPlan& P, const uint8_t* d_ta
     CUDA_TRY(prof_mark(h, h->opt.ssim_window == QMIV_SSIM_GAUSS11 ? "k_ssim<11>" : "k_ssim<10>", st, true));
     CUDA_TRY(launch_ssim(d_sjobs, h->sjobs.data(), (int)h->sjobs.size(), h->opt.ssim_window, st));
     CUDA_TRY(prof_mark(h, nullptr, st, false));
-    h->launches += 2;
+    h->launches += 2 + (ssim_tiles(h->sjobs) > 0 ? 1 : 0);  // the tile kernel (if any tiles), two finalisation passes
     CUDA_TRY(launch_ssim_combine(d_frames, (int)h->frames.size(), h->params, st));
     h->launches++;
   }
@@ -1780,7 +1788,7 @@ qmiv_status qmiv_ssim(qmiv_handle* h, const qmiv_pic* tst, const qmiv_pic* ref, 
   const SsimJob* d_sjobs = reinterpret_cast<const SsimJob*>(h->d_tab + h->tab.jobs_off);
   h->prof_n = 0;
   CUDA_TRY(launch_ssim(d_sjobs, h->sjobs.data(), 3, h->opt.ssim_window, st));
-  h->launches += 2;
+  h->launches += 2 + (ssim_tiles(h->sjobs) > 0 ? 1 : 0);
   double v[3];
   CUDA_TRY(cudaMemcpyAsync(v, h->slots[0].vals, sizeof(v), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaStreamSynchronize(st));
