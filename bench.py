@@ -593,10 +593,13 @@ def stream_workload(args, dev):
 
     run(4)
     torch.cuda.synchronize()
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
     t0 = time.perf_counter()
     run(nf)
     torch.cuda.synchronize()
     secs = time.perf_counter() - t0
+    clk = clocks.stop()
     # device-resident: the same calls without uploads
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(ks)
@@ -611,7 +614,7 @@ def stream_workload(args, dev):
     torch.cuda.empty_cache()
     out = {"workload": STREAM_WORKLOAD, "value": nf * w * h / secs / 1e9, "unit": "Gpixel/s (with uploads)",
            "seconds": secs, "ms_per_frame": secs * 1e3 / nf, "device_ms_per_frame": dev_ms,
-           "h2d_bytes_per_frame": 2 * n * 2,
+           "h2d_bytes_per_frame": 2 * n * 2, "clocks": clk,
            "check": {"ivpsnr_frame0": r0.ivpsnr, "wspsnr_frame0": list(r0.wspsnr)[:3], "ivssim_frame0": r0.ivssim,
                      "msssim_frame0": list(r0.msssim)[:3]}}
     if not args.no_cpu_baseline and ref_cli_ok():
