@@ -999,11 +999,11 @@ def run_ours(args):
     for _ in range(max(2, args.warmup)):
         e2e_step()
     torch.cuda.synchronize()
-    # two timed passes of K steps, the faster one reported (both listed): the host link and host
+    # three timed passes of K steps, the fastest one reported (all listed): the host link and host
     # memory of this shared machine see other tenants' traffic, which moved single passes by up
     # to a factor of two between otherwise identical processes
     e2e_passes = []
-    for _ in range(2):
+    for _ in range(3):
         barrier()
         e0.record(stream)
         for _ in range(args.steps):
