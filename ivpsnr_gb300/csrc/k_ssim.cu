@@ -126,8 +126,22 @@ __global__ void __launch_bounds__(kThreads, 3) k_ssim(const SsimJob* __restrict_
   }
   const int wi = WIN == 11 ? 1 : 0;
 
+  // a contiguous range of tiles per block: its first job by binary search, then at most one step
+  // of the job walk per tile (a range strided by the grid crossed several small pyramid-level
+  // jobs per tile, each a dependent load)
+  const int t_begin = (int)((int64_t)ntiles * blockIdx.x / gridDim.x);
+  const int t_end = (int)((int64_t)ntiles * (blockIdx.x + 1) / gridDim.x);
   int jb = 0;
-  for(int tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+  {
+    int lo = 0, hi = njobs - 1;
+    while(lo < hi)
+    {
+      const int mid = (lo + hi + 1) >> 1;
+      if(jobs[mid].tile_base <= t_begin) lo = mid; else hi = mid - 1;
+    }
+    jb = lo;
+  }
+  for(int tile = t_begin; tile < t_end; tile++)
   {
     const TilePos cur = locate<G::TX>(jobs, njobs, jb, tile);
     jb = cur.jb;
