@@ -1044,7 +1044,8 @@ def run_ours(args):
                     "call": "qmiv_calc_batch_host (pinned host pictures, grouped uploads overlapped with compute)"},
             "gpu_launches": gpu_launches,
             # the search kernel is bound by integer instruction issue: three views side by side.
-            # frac: the reference formulation's integer ops (9 per candidate) over the
+            # frac: the reference formulation's integer ops (per candidate: 3 differences, 3 squares,
+            # 2 weighted adds and a compare-select, 9; xCorrespPixelShiftSTD.cpp:41-75) over the
             # INT32 lane rate (above 1: the expanded-key search executes fewer instructions than that
             # formulation counts); issue_frac: the warp instructions it does execute (ncu count per
             # pixel) over the 4-per-cycle issue rate, i.e. the headroom left; hbm_frac: its input
