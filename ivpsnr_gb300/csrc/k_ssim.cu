@@ -719,7 +719,8 @@ __global__ void __launch_bounds__(kFinThreads) k_ssim_fin_jobs(const SsimJob* __
   for(int r = threadIdx.x; r < rows; r += kFinThreads)
   {
     const float* pr = J.partial + (int64_t)r * tx;
-    k = kbns_add(k, tx >= 2 ? __dadd_rn((double)__ldcg(pr), (double)__ldcg(pr + 1)) : (double)__ldcg(pr));
+    // a row of no tiles (a plane at most 10 wide) contributes 0
+    k = kbns_add(k, tx >= 2 ? __dadd_rn((double)__ldcg(pr), (double)__ldcg(pr + 1)) : (tx == 1 ? (double)__ldcg(pr) : 0.0));
   }
   const double tot = block_kbns(k, scratch);
   if(threadIdx.x == 0) *J.out = __ddiv_rn(tot, (double)((int64_t)J.W * J.H));

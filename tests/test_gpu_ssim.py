@@ -96,6 +96,22 @@ def test_ssim_444_and_tiny(gpu_lib, oq):
                          gpu_lib.M_MSSSIM)
 
 
+def test_msssim_level_without_window_columns(gpu_lib, oq):
+    """96x320: MS-SSIM level 4 is 6x20, rows but no window columns; those rows add nothing (the
+    oracle's MS-SSIM is 0), also after a larger call has left other values in the handle's
+    per-tile sums."""
+    w, h, bd = 96, 320, 10
+    ref, tst = synth.pair420(w, h, bd, seed=11, holes=True)
+    o, _, _ = _oracle(oq, ref, tst, w, h, bd)
+    assert o["msssim"] == [0.0, 0.0, 0.0]
+    big_ref, big_tst = synth.pair420(256, 320, bd, seed=12, holes=True)
+    with gpu_lib.Processor(256, 320) as P:
+        P.calc_frame(gpu_lib.make_pic(_planes(big_ref, 256, 320), bd), gpu_lib.make_pic(_planes(big_tst, 256, 320), bd),
+                     gpu_lib.M_ALL)
+        g = P.calc_frame(gpu_lib.make_pic(_planes(ref, w, h), bd), gpu_lib.make_pic(_planes(tst, w, h), bd), gpu_lib.M_ALL)
+    _cmp_ssim(g, o)
+
+
 def test_standalone_ssim_call(gpu_lib, oq):
     from ivpsnr_gb300 import _abi
     w, h, bd = 256, 144, 10
