@@ -40,6 +40,8 @@ CASES = [
     (1920, 1080, 8, synth.seed_for(0, 0, 0), False, 0),
     (1920, 1080, 10, synth.seed_for(2, 0, 0), True, 0),
     (640, 360, 10, 101, True, 1),
+    (1920, 1080, 12, 106, True, 1),    # 12-bit at full HD, Gaussian window
+    (1920, 1080, 14, 107, True, 0),    # 14-bit: the 64-bit-key search variants
     (130, 66, 8, 102, False, 0),
     (96, 64, 12, 103, False, 0),
     (64, 48, 14, 104, False, 1),
