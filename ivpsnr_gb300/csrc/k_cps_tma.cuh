@@ -10,8 +10,10 @@
 //     and chroma is read straight from the raw box through clamped indices;
 //   * each warp walks 2x2 quads of one direction down its rows in a compact loop: per
 //     quad, 9 chroma costs (the quad's window covers 3x3 chroma samples), then 2B+2
-//     reference rows x 2 output rows x 2 columns x (2B+1) candidates of one
-//     multiply-add + add + unsigned min each;
+//     reference rows, each turned once into z = R^2 + B + kk for the quad, and per pixel and
+//     candidate one multiply-add and a share of a three-way minimum (the expanded 32-bit key
+//     below; the 64-bit-key shapes evaluate the key directly); the argmin's reference samples
+//     are read back from the raw box inside the picture;
 //   * per-row squared errors are reduced with a single warp reduction per row and
 //     component per chunk, kept in one lane's register for the whole block, and added to the
 //     job's row sums once at the end.
